@@ -1,0 +1,275 @@
+"""ctypes binding of the FP64 CPU oracle (liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+cpu_baseline leg of bench.py, always as the checker.  The product never
+imports it.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+JACOBI, SERIAL = 0, 1
+DIST_EUC_2D, DIST_GEO, DIST_EUC_2D_FLOAT = 0, 1, 2
+
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+
+
+class Csr(C.Structure):
+    _fields_ = [("n", C.c_int64), ("nnz", C.c_int64), ("rowptr", C.c_void_p),
+                ("col", C.c_void_p), ("val", C.c_void_p), ("wsum", C.c_double)]
+
+
+class Params(C.Structure):
+    _fields_ = [("dt", C.c_double), ("steps", C.c_int32), ("agents", C.c_int32),
+                ("fused", C.c_int32), ("uw", C.c_int32), ("period", C.c_int32),
+                ("threshold", C.c_int32), ("seed", C.c_uint32),
+                ("schedule", C.c_int32), ("nthreads", C.c_int32)]
+
+
+class Result(C.Structure):
+    _fields_ = [("min", C.c_double), ("max", C.c_double), ("mean", C.c_double),
+                ("std", C.c_double), ("ps", C.c_double), ("xi0", C.c_double),
+                ("steps_run", C.c_int64), ("windows_run", C.c_int64),
+                ("bifurcated", C.c_int64), ("valid", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        _lib = C.CDLL(LIB_PATH)
+        _lib.sbo_xi0.restype = C.c_double
+        _lib.sbo_tsp_tour_length.restype = C.c_double
+        _lib.sbo_dense_to_csr.restype = C.c_int64
+    return _lib
+
+
+class Graph:
+    """A CSR matrix held in numpy arrays, with the reference's weight sum W."""
+
+    def __init__(self, n, rowptr, col, val, wsum):
+        self.n = int(n)
+        self.rowptr = np.ascontiguousarray(rowptr, dtype=np.int32)
+        self.col = np.ascontiguousarray(col, dtype=np.int32)
+        self.val = np.ascontiguousarray(val, dtype=np.float64)
+        self.wsum = float(wsum)
+
+    @property
+    def nnz(self):
+        return int(self.col.size)
+
+    def cstruct(self):
+        return Csr(self.n, self.nnz, self.rowptr.ctypes.data, self.col.ctypes.data,
+                   self.val.ctypes.data, self.wsum)
+
+
+def params(dt=0.1, steps=10000, agents=1024, fused=1, uw=0, period=100,
+           threshold=25, seed=1234, schedule=JACOBI, nthreads=0):
+    return Params(dt, steps, agents, fused, uw, period, threshold, seed, schedule,
+                  nthreads)
+
+
+def rand_stream(seed, count):
+    out = np.empty(count, np.int32)
+    lib().sbo_rand_stream(C.c_uint32(seed), C.c_int64(count), out.ctypes.data_as(C.c_void_p))
+    return out
+
+
+def xi0(g):
+    c = g.cstruct()
+    return lib().sbo_xi0(C.byref(c))
+
+
+def init_maxcut(n, A, seed):
+    x = np.empty(n * A)
+    y = np.empty(n * A)
+    lib().sbo_init_maxcut(C.c_int64(n), C.c_int64(A), C.c_uint32(seed),
+                          x.ctypes.data_as(C.c_void_p), y.ctypes.data_as(C.c_void_p))
+    return x, y
+
+
+def fused_step(g, x, y, A, step, max_steps, dt, xi0v, schedule=JACOBI, nthreads=0):
+    c = g.cstruct()
+    lib().sbo_fused_step(C.byref(c), x.ctypes.data_as(C.c_void_p),
+                         y.ctypes.data_as(C.c_void_p), C.c_int64(A), C.c_int32(step),
+                         C.c_int32(max_steps), C.c_double(dt), C.c_double(xi0v),
+                         C.c_int(schedule), C.c_int(nthreads))
+
+
+def update_xy(x, y, step, max_steps, dt):
+    lib().sbo_update_xy(x.ctypes.data_as(C.c_void_p), y.ctypes.data_as(C.c_void_p),
+                        C.c_int64(x.size), C.c_int32(step), C.c_int32(max_steps),
+                        C.c_double(dt))
+
+
+def unfused_step(g, x, y, A, step, max_steps, dt, xi0v):
+    c = g.cstruct()
+    lib().sbo_unfused_step(C.byref(c), x.ctypes.data_as(C.c_void_p),
+                           y.ctypes.data_as(C.c_void_p), C.c_int64(A), C.c_int32(step),
+                           C.c_int32(max_steps), C.c_double(dt), C.c_double(xi0v))
+
+
+def init_tsp(n, A, seed):
+    x = np.empty(n * A)
+    y = np.empty(n * A)
+    lib().sbo_init_tsp(C.c_int64(n), C.c_int64(A), C.c_uint32(seed),
+                       x.ctypes.data_as(C.c_void_p), y.ctypes.data_as(C.c_void_p))
+    return x, y
+
+
+def cut(g, spins, A):
+    c = g.cstruct()
+    spins = np.ascontiguousarray(spins, dtype=np.int32)
+    out = np.empty(A)
+    lib().sbo_cut(C.byref(c), spins.ctypes.data_as(C.c_void_p), C.c_int64(A),
+                  out.ctypes.data_as(C.c_void_p))
+    return out
+
+
+def maxcut_solve(g, p, want_state=False):
+    c = g.cstruct()
+    A = p.agents
+    r = Result()
+    cutv = np.empty(A)
+    x = np.empty(g.n * A) if want_state else None
+    y = np.empty(g.n * A) if want_state else None
+    s = np.empty(g.n * A, np.int32) if want_state else None
+    vp = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)
+    rc = lib().sbo_maxcut_solve(C.byref(c), C.byref(p), C.byref(r), vp(cutv), vp(x),
+                                vp(y), vp(s))
+    if rc != 0:
+        raise ValueError("sbo_maxcut_solve failed: %d" % rc)
+    out = {"result": r.as_dict(), "cut": cutv}
+    if want_state:
+        out.update(x=x, y=y, spins=s)
+    return out
+
+
+def mtx_load(path):
+    n = C.c_int64()
+    nnz = C.c_int64()
+    w = C.c_double()
+    rc = lib().sbo_mtx_load(path.encode(), C.byref(n), C.byref(nnz), None, None, None,
+                            C.byref(w))
+    if rc != 0:
+        raise ValueError("sbo_mtx_load(%s) failed: %d" % (path, rc))
+    rp = np.empty(n.value + 1, np.int32)
+    col = np.empty(nnz.value, np.int32)
+    val = np.empty(nnz.value)
+    rc = lib().sbo_mtx_load(path.encode(), C.byref(n), C.byref(nnz),
+                            rp.ctypes.data_as(C.c_void_p), col.ctypes.data_as(C.c_void_p),
+                            val.ctypes.data_as(C.c_void_p), C.byref(w))
+    return Graph(n.value, rp, col, val, w.value)
+
+
+def tsplib_load(path):
+    N = C.c_int32()
+    kind = C.c_int()
+    rc = lib().sbo_tsplib_load(path.encode(), C.byref(N), None, None, C.byref(kind))
+    if rc != 0:
+        raise ValueError("sbo_tsplib_load(%s) failed: %d" % (path, rc))
+    xc = np.empty(N.value)
+    yc = np.empty(N.value)
+    rc = lib().sbo_tsplib_load(path.encode(), C.byref(N), xc.ctypes.data_as(C.c_void_p),
+                               yc.ctypes.data_as(C.c_void_p), C.byref(kind))
+    if rc != 0:
+        raise ValueError("sbo_tsplib_load(%s) failed: %d" % (path, rc))
+    return xc, yc, kind.value
+
+
+class Tsp:
+    """TSP instance: packed distances, per-city sums, the QUBO as CSR."""
+
+    def __init__(self, xc, yc, kind, A=1.0, B=None, C_=None, penalty_scale=1.0):
+        self.N = N = int(len(xc))
+        self.kind = kind
+        self.xc = np.ascontiguousarray(xc, np.float64)
+        self.yc = np.ascontiguousarray(yc, np.float64)
+        self.packed = np.empty(N * (N - 1) // 2)
+        rc = lib().sbo_tsp_distances(C.c_int32(N), self.xc.ctypes.data_as(C.c_void_p),
+                                     self.yc.ctypes.data_as(C.c_void_p), C.c_int(kind),
+                                     self.packed.ctypes.data_as(C.c_void_p))
+        if rc != 0:
+            raise ValueError("bad TSP instance")
+        self.rowsum = np.empty(N)
+        mx = C.c_double()
+        sm = C.c_double()
+        lib().sbo_tsp_rowsums(C.c_int32(N), self.packed.ctypes.data_as(C.c_void_p),
+                              self.rowsum.ctypes.data_as(C.c_void_p), C.byref(mx),
+                              C.byref(sm))
+        self.maxd = mx.value
+        self.qa = float(A)
+        self.qb = float(B) if B is not None else penalty_scale * mx.value
+        self.qc = float(C_) if C_ is not None else penalty_scale * mx.value
+        m = N * N
+        dense = np.empty(m * m)
+        lib().sbo_tsp_qubo_dense(C.c_int32(N), self.packed.ctypes.data_as(C.c_void_p),
+                                 C.c_double(self.qa), C.c_double(self.qb),
+                                 C.c_double(self.qc), dense.ctypes.data_as(C.c_void_p))
+        nnz = lib().sbo_dense_to_csr(C.c_int64(m), dense.ctypes.data_as(C.c_void_p),
+                                     None, None, None)
+        rp = np.empty(m + 1, np.int32)
+        col = np.empty(nnz, np.int32)
+        val = np.empty(nnz)
+        lib().sbo_dense_to_csr(C.c_int64(m), dense.ctypes.data_as(C.c_void_p),
+                               rp.ctypes.data_as(C.c_void_p), col.ctypes.data_as(C.c_void_p),
+                               val.ctypes.data_as(C.c_void_p))
+        self.graph = Graph(m, rp, col, val, 0.0)
+
+    def tour_length(self, tour):
+        t = np.ascontiguousarray(tour, np.int32)
+        return lib().sbo_tsp_tour_length(C.c_int32(self.N),
+                                         self.packed.ctypes.data_as(C.c_void_p),
+                                         t.ctypes.data_as(C.c_void_p))
+
+    def step(self, x, y, A, step, max_steps, dt, schedule=JACOBI):
+        c = self.graph.cstruct()
+        lib().sbo_tsp_step(C.byref(c), self.rowsum.ctypes.data_as(C.c_void_p),
+                           x.ctypes.data_as(C.c_void_p), y.ctypes.data_as(C.c_void_p),
+                           C.c_int64(A), C.c_int32(step), C.c_int32(max_steps),
+                           C.c_double(dt), C.c_double(0.002), C.c_int32(self.N),
+                           C.c_double(self.qa), C.c_double(self.qb), C.c_double(self.qc),
+                           C.c_int(schedule))
+
+    def solve(self, p, want_state=False):
+        c = self.graph.cstruct()
+        A = p.agents
+        r = Result()
+        lengths = np.empty(A)
+        tours = np.full(A * self.N, -1, np.int32)
+        valid = np.empty(A, np.int32)
+        n = self.N * self.N
+        x = np.empty(n * A) if want_state else None
+        y = np.empty(n * A) if want_state else None
+        vp = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)
+        rc = lib().sbo_tsp_solve(C.byref(c), C.c_int32(self.N),
+                                 self.packed.ctypes.data_as(C.c_void_p),
+                                 self.rowsum.ctypes.data_as(C.c_void_p),
+                                 C.c_double(self.qa), C.c_double(self.qb),
+                                 C.c_double(self.qc), C.byref(p), C.byref(r),
+                                 vp(lengths), vp(tours), vp(x), vp(y), vp(valid))
+        if rc != 0:
+            raise ValueError("sbo_tsp_solve failed: %d" % rc)
+        out = {"result": r.as_dict(), "lengths": lengths,
+               "tours": tours.reshape(A, self.N), "valid": valid}
+        if want_state:
+            out.update(x=x, y=y)
+        return out
