@@ -1,0 +1,172 @@
+/*
+ * sbx.h -- C ABI of the GB300 simulated-bifurcation (SB) engine.
+ *
+ * Plain C: pointers, sizes and POD structs; no CUDA or C++ types cross this
+ * boundary.  Every call returns SBX_OK (0) or a negative status (sbx_strerror
+ * names it); nothing calls exit().  Host buffers belong to the caller and are
+ * copied; device buffers belong to the context.  One context per host thread.
+ *
+ * It replaces the reference's class interface (Sparse-Ising-Solver):
+ *   sbx_problem_csr   <- CSR(string) + CSR_GPU(CSR&)          src/csr.cuh:26-47,89-95
+ *   sbx_problem_tsp   <- TSP_GPU(TSP_CPU&) + construct_matrix  src/csr.cuh:65-87
+ *   sbx_solve (MaxCut)<- Ising::Ising + Ising::symplectic_update
+ *                                                             src/csr.cuh:97-104
+ *   sbx_solve (TSP)   <- Ising_TSP::Ising_TSP + symplectic_update
+ *                                                             src/csr.cuh:156-163
+ *   sbx_load_mtx      <- CSR::from_file                       src/csr.cpp:15-109
+ *   sbx_load_tsplib   <- TSP_CPU::read_file                   src/tsp_cpu.cpp:9-45
+ *   sbx_tsp_distances <- TSP_distances_EUC_2D / _GEO          src/kernels.cu:404-442
+ * The `program` CLI built beside libsbx.so keeps src/main.cu:255-312's
+ * arguments and the output-file line of src/ising.cu:267 + src/main.cu:223.
+ */
+#ifndef SBX_H
+#define SBX_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define SBX_OK 0
+#define SBX_ERR_ARG (-1)         /* invalid argument */
+#define SBX_ERR_CUDA (-2)        /* a CUDA runtime call failed */
+#define SBX_ERR_NOMEM (-3)       /* host or device allocation failed */
+#define SBX_ERR_IO (-4)          /* file cannot be opened or read */
+#define SBX_ERR_FORMAT (-5)      /* malformed .mtx / .tsp file */
+#define SBX_ERR_UNSUPPORTED (-6) /* valid request this build cannot serve */
+#define SBX_ERR_NODEVICE (-7)    /* no usable CUDA device */
+#define SBX_ERR_STATE (-8)       /* call out of order (e.g. no solve yet) */
+
+/* agent-state storage precision (arithmetic of the force is exact) */
+enum { SBX_F32 = 0, SBX_BF16 = 1, SBX_F16 = 2, SBX_F64 = 3 };
+/* kernel family: chosen by shape (AUTO) or forced */
+enum { SBX_KERNEL_AUTO = 0, SBX_KERNEL_STREAM = 1, SBX_KERNEL_RESIDENT = 2 };
+/* TSP distance kinds, src/kernels.cu:404-442 */
+enum { SBX_DIST_EUC_2D = 0, SBX_DIST_GEO = 1, SBX_DIST_EUC_2D_FLOAT = 2 };
+/* sbx_params.flags */
+#define SBX_FLAG_NO_PDL 1u      /* launch without programmatic dependent launch */
+#define SBX_FLAG_NO_GRAPH 2u    /* launch kernels directly, not through a graph */
+#define SBX_FLAG_PROFILE 4u     /* time every hot-kernel launch with events */
+
+typedef struct sbx_ctx sbx_ctx;
+typedef struct sbx_problem sbx_problem;
+
+typedef struct sbx_params {
+    double dt;              /* time_step; reference default 0.1 (main.cu:272) */
+    int32_t steps;          /* max_steps; reference default 10000 */
+    int32_t agents;         /* columns of X; reference default 1024 */
+    int32_t fused;          /* 1: fused step kernel (default); 0: unfused trio */
+    int32_t update_window;  /* MaxCut early exit once every agent bifurcated */
+    int32_t period;         /* steps per window; 0: reference (100 / steps/10) */
+    int32_t threshold;      /* window convergence threshold; 0: reference (25 / 50) */
+    int32_t precision;      /* SBX_F32 (default), SBX_BF16, SBX_F16, SBX_F64 */
+    uint32_t seed;          /* srand() seed of the reference's init stream */
+    int32_t kernel;         /* SBX_KERNEL_* */
+    int32_t agents_per_block; /* resident kernel tile; 0: autotuned */
+    int32_t trace;          /* 1: record the best cut at every window */
+    uint32_t flags;         /* SBX_FLAG_* */
+} sbx_params;
+
+typedef struct sbx_result {
+    double time_us;         /* SB loop wall time: pre-step .. last window done */
+    double min, max, mean, std, ps; /* MaxCut: cuts (ising.cu:238-265);
+                                       TSP: tour lengths of valid agents */
+    double xi0;
+    int64_t steps_run;      /* SB steps after the pre-step */
+    int64_t windows_run;
+    int64_t bifurcated;     /* agents whose bifurcated flag is set */
+    int64_t valid;          /* TSP: agents holding a valid tour */
+    int32_t best_agent;     /* first agent reaching max (MaxCut) / min (TSP) */
+    int32_t kernel_used;    /* SBX_KERNEL_STREAM or SBX_KERNEL_RESIDENT */
+    int32_t agents_per_block;
+    int32_t reserved;
+    double kernel_ms;       /* SBX_FLAG_PROFILE: summed hot-kernel time */
+    int64_t kernel_launches;/* hot-kernel launches issued by the solve */
+    int64_t gpu_launches;   /* all kernel launches issued by the solve */
+} sbx_result;
+
+const char *sbx_strerror(int status);
+/* Text of the last failure on this thread (empty when none). */
+const char *sbx_last_error(void);
+const char *sbx_version(void);
+/* Reference defaults (main.cu:269-274 with dt 0.1). */
+void sbx_params_default(sbx_params *p);
+
+int sbx_create(sbx_ctx **ctx, int device);
+int sbx_destroy(sbx_ctx *ctx);
+/* Run on a caller's cudaStream_t (passed as void*); NULL selects the
+ * context's own stream. */
+int sbx_set_stream(sbx_ctx *ctx, void *cuda_stream);
+
+/* MaxCut / Ising problem from host CSR arrays (copied).  weight_sum is the
+ * reference's csr.sum (one triangle of the file's weights). */
+int sbx_problem_csr(sbx_ctx *ctx, int64_t n, int64_t nnz, const int32_t *rowptr,
+                    const int32_t *col, const double *val, double weight_sum,
+                    sbx_problem **out);
+/* TSP-QUBO problem from packed upper-triangular distances (N(N-1)/2), the
+ * distance weight A and the row/column penalties B, C (tsp_gpu.cu:76-112). */
+int sbx_problem_tsp(sbx_ctx *ctx, int32_t ncities, const double *packed_dist,
+                    double A, double B, double C, sbx_problem **out);
+int sbx_problem_destroy(sbx_problem *p);
+int sbx_problem_info(const sbx_problem *p, int64_t *n, int64_t *nnz,
+                     int32_t *is_tsp);
+
+/* One SB run.  agent_values (optional, [agents]) receives each agent's cut
+ * (MaxCut) or tour length (TSP, NaN when the agent holds no valid tour). */
+int sbx_solve(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *params,
+              sbx_result *res, double *agent_values);
+/* State of the last solve, [n*agents] each, row-major (row*agents+agent);
+ * spins are the window spins (current_spins) as +1/-1.  NULL skips. */
+int sbx_get_state(sbx_ctx *ctx, double *x, double *y, int32_t *spins);
+/* TSP tours of the last solve: tours[agents*N] (city order, -1 when the agent
+ * has no valid tour) and valid_step[agents] (ising_tsp.cu valid_list). */
+int sbx_get_tours(sbx_ctx *ctx, int32_t *tours, int32_t *valid_step);
+/* Best cut after each window of the last solve (params.trace = 1). */
+int sbx_get_trace(sbx_ctx *ctx, int64_t cap, int64_t *steps, double *best,
+                  int64_t *count);
+
+/* ---- batched MaxCut: many independent instances, one launch per step ---- */
+/* Each instance keeps its own xi0, weight sum and agent count; all share
+ * dt/steps/precision from params.  Per-instance results go to res[count]
+ * and agent_values (concatenated, sum of agents) when given. */
+int sbx_solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems,
+                    const int32_t *agents, const sbx_params *params,
+                    sbx_result *res, double *agent_values, double *batch_time_us);
+
+/* ---- host-side loaders (no device needed) ---- */
+/* csr.cpp:15-109: two-call protocol, first with NULL arrays for the sizes. */
+int sbx_load_mtx(const char *path, int64_t *n, int64_t *nnz, int32_t *rowptr,
+                 int32_t *col, double *val, double *weight_sum);
+/* tsp_cpu.cpp:9-45: two-call protocol on xc / yc. */
+int sbx_load_tsplib(const char *path, int32_t *ncities, double *xc, double *yc,
+                    int32_t *kind);
+/* kernels.cu:404-442 on the host: packed distances of N cities. */
+int sbx_tsp_distances(int32_t ncities, const double *xc, const double *yc,
+                      int32_t kind, double *packed);
+
+/* ---- seeded synthetic instances (host; two-call like sbx_load_mtx) ---- */
+/* Erdos-Renyi G(n, p), weights +1, or +-1 uniform when pm1 != 0. */
+int sbx_gen_er(int64_t n, double p, int32_t pm1, uint64_t seed, int64_t *nnz,
+               int32_t *rowptr, int32_t *col, double *val, double *weight_sum);
+/* rows x cols 2-D torus, degree 4, weights +-1 uniform per edge. */
+int sbx_gen_torus(int32_t rows, int32_t cols, uint64_t seed, int64_t *nnz,
+                  int32_t *rowptr, int32_t *col, double *val, double *weight_sum);
+/* R-MAT, 2^scale vertices, edge_factor*2^scale edge draws, (a, b, c),
+ * self loops and duplicates removed, weights +1, empty rows kept. */
+int sbx_gen_rmat(int32_t scale, int32_t edge_factor, double a, double b,
+                 double c, uint64_t seed, int64_t *nnz, int32_t *rowptr,
+                 int32_t *col, double *val, double *weight_sum);
+/* Random geometric graph in the unit square with the radius that gives
+ * avg_degree, weights +-1 uniform. */
+int sbx_gen_rgg(int64_t n, double avg_degree, uint64_t seed, int64_t *nnz,
+                int32_t *rowptr, int32_t *col, double *val, double *weight_sum);
+/* ncities uniform in [0, scale)^2. */
+int sbx_gen_cities(int32_t ncities, double scale, uint64_t seed, double *xc,
+                   double *yc);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

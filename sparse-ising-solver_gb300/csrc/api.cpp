@@ -1,0 +1,932 @@
+// api.cpp -- the C ABI (include/sbx.h): contexts, problems, solves.
+//
+// Host orchestration of one MaxCut solve follows Ising::symplectic_update
+// (src/ising.cu:140-271): init from the seed, the pre-step Update_XY, windows
+// of `period` steps, the optional all-bifurcated early exit, the cut of the
+// window spins and the statistics line.  The TSP solve follows
+// Ising_TSP::symplectic_update (src/ising_tsp.cu:111-253).  Every CUDA error
+// becomes a negative status; nothing exits the process.
+#include "../../include/sbx.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+
+using namespace sbx;
+
+struct sbx_problem {
+    sbx_ctx *ctx = nullptr;
+    bool tsp = false;
+    DevCsr J;
+    DevTsp T;
+};
+
+struct sbx_ctx {
+    int device = 0;
+    cudaStream_t own = nullptr, stream = nullptr;
+    Work w;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evp[4] = {};
+    int32_t *pinned = nullptr;   // stop-flag ring for the update-window poll
+    // graph cache for the streaming chunk
+    cudaGraphExec_t gexec = nullptr;
+    std::string gkey;
+    std::vector<cudaEvent_t> prof;   // SBX_FLAG_PROFILE: events around step kernels
+    // last solve
+    bool have = false, last_tsp = false;
+    SolveDims d;
+    int32_t N = 0;
+    std::string err;
+};
+
+namespace {
+
+thread_local std::string g_err;
+uint64_t g_alloc_gen = 0;   // bumped by every (re)allocation of a work buffer
+
+int fail(sbx_ctx *c, int code, const std::string &m)
+{
+    if (c) c->err = m;
+    g_err = m;
+    return code;
+}
+
+#define CK(call)                                                                   \
+    do {                                                                           \
+        cudaError_t e_ = (call);                                                   \
+        if (e_ != cudaSuccess)                                                     \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? SBX_ERR_NOMEM : SBX_ERR_CUDA, \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));       \
+    } while (0)
+
+template <class T> cudaError_t grow(T *&p, size_t &cap, size_t count)
+{
+    size_t bytes = count * sizeof(T);
+    if (bytes == 0) bytes = sizeof(T);
+    if (cap >= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc((void **)&p, bytes);
+    if (e == cudaSuccess) cap = bytes;
+    g_alloc_gen++;
+    return e;
+}
+
+cudaError_t growv(void *&p, size_t &cap, size_t bytes)
+{
+    if (bytes == 0) bytes = 16;
+    if (cap >= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e == cudaSuccess) cap = bytes;
+    g_alloc_gen++;
+    return e;
+}
+
+void free_csr(DevCsr &J)
+{
+    cudaFree(J.rowptr);
+    cudaFree(J.colw);
+    cudaFree(J.vald);
+    cudaFree(J.valf);
+    cudaFree(J.perm);
+    J.rowptr = nullptr;
+    J.colw = nullptr;
+    J.vald = nullptr;
+    J.valf = nullptr;
+    J.perm = nullptr;
+}
+
+// Upload a validated CSR; classify its weights.
+int upload_csr(sbx_ctx *ctx, DevCsr &J, int64_t n, int64_t nnz, const int32_t *rowptr,
+               const int32_t *col, const double *val, double wsum)
+{
+    if (n <= 0 || n > INT32_MAX - 1 || nnz < 0 || nnz > INT32_MAX || !rowptr || (nnz && (!col || !val)))
+        return fail(ctx, SBX_ERR_ARG, "bad CSR sizes or pointers");
+    if (rowptr[0] != 0 || rowptr[n] != nnz) return fail(ctx, SBX_ERR_ARG, "rowptr[0] != 0 or rowptr[n] != nnz");
+    int32_t maxdeg = 0;
+    for (int64_t r = 0; r < n; r++) {
+        if (rowptr[r + 1] < rowptr[r]) return fail(ctx, SBX_ERR_ARG, "rowptr not monotone");
+        maxdeg = std::max(maxdeg, rowptr[r + 1] - rowptr[r]);
+    }
+    bool unit = true, integer = true;
+    double rowabs_max = 0;
+    std::vector<uint32_t> colw((size_t)nnz);
+    std::vector<float> valf((size_t)nnz);
+    for (int64_t r = 0; r < n; r++) {
+        double ra = 0;
+        for (int32_t e = rowptr[r]; e < rowptr[r + 1]; e++) {
+            if (col[e] < 0 || col[e] >= n) return fail(ctx, SBX_ERR_ARG, "column index out of range");
+            const double v = val[e];
+            if (!std::isfinite(v)) return fail(ctx, SBX_ERR_ARG, "non-finite weight");
+            if (std::fabs(v) != 1.0) unit = false;
+            if (v != std::floor(v) || std::fabs(v) > 16777216.0) integer = false;
+            ra += std::fabs(v);
+            valf[e] = (float)v;
+        }
+        rowabs_max = std::max(rowabs_max, ra);
+    }
+    if (rowabs_max >= 2147483647.0) integer = false;
+    for (int64_t e = 0; e < nnz; e++)
+        colw[e] = (uint32_t)col[e] | ((unit && val[e] < 0) ? 0x80000000u : 0u);
+    // rows by decreasing degree: a warp of the resident kernel gets rows of
+    // similar length
+    std::vector<int32_t> perm((size_t)n);
+    std::iota(perm.begin(), perm.end(), 0);
+    std::stable_sort(perm.begin(), perm.end(), [&](int32_t a, int32_t b) {
+        return rowptr[a + 1] - rowptr[a] > rowptr[b + 1] - rowptr[b];
+    });
+    J.n = n;
+    J.nnz = nnz;
+    J.unit = unit;
+    J.integer = integer;
+    J.wsum = wsum;
+    J.max_deg = maxdeg;
+    J.hval.assign(val, val + nnz);
+    J.hrowptr.assign(rowptr, rowptr + n + 1);
+    J.hcol.assign(col, col + nnz);
+    CK(cudaMalloc(&J.rowptr, sizeof(int32_t) * (n + 1)));
+    CK(cudaMalloc(&J.colw, sizeof(uint32_t) * std::max<int64_t>(nnz, 1)));
+    CK(cudaMalloc(&J.vald, sizeof(double) * std::max<int64_t>(nnz, 1)));
+    CK(cudaMalloc(&J.valf, sizeof(float) * std::max<int64_t>(nnz, 1)));
+    CK(cudaMalloc(&J.perm, sizeof(int32_t) * n));
+    CK(cudaMemcpy(J.rowptr, rowptr, sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice));
+    if (nnz) {
+        CK(cudaMemcpy(J.colw, colw.data(), sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(J.vald, val, sizeof(double) * nnz, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(J.valf, valf.data(), sizeof(float) * nnz, cudaMemcpyHostToDevice));
+    }
+    CK(cudaMemcpy(J.perm, perm.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+    return SBX_OK;
+}
+
+// src/ising.cu:103-125 (with n*n formed in double).
+double xi0_of(const DevCsr &J)
+{
+    const double nn = (double)J.n * (double)J.n;
+    double sum = 0.0;
+    for (double v : J.hval) sum += v;
+    const double mean = sum / nn;
+    double nonzero = 0.0;
+    for (double v : J.hval) nonzero += std::pow(v - mean, 2);
+    const double zero = (nn - (double)J.nnz) * mean * mean;
+    sum = nonzero + zero;
+    const double sigma = std::pow(sum / (nn - 1.0), 0.5);
+    return 0.7 / (sigma * std::pow((double)J.n, 0.5));
+}
+
+// ising.cu:238-265 (MaxCut) -- the reference's loop, so the statistics are
+// bit-identical for identical per-agent values.
+void stats(const std::vector<double> &v, sbx_result *r)
+{
+    const int64_t A = (int64_t)v.size();
+    double mx = -DBL_MAX, mn = DBL_MAX, total = 0, sd = 0;
+    for (double x : v) {
+        if (x > mx) mx = x;
+        if (x < mn) mn = x;
+        total += x;
+    }
+    const double avg = total / A;
+    int64_t nmax = 0;
+    int32_t best = -1;
+    for (int64_t i = 0; i < A; i++) {
+        sd += std::pow(v[i] - avg, 2);
+        if (v[i] == mx) {
+            nmax++;
+            if (best < 0) best = (int32_t)i;
+        }
+    }
+    r->min = mn;
+    r->max = mx;
+    r->mean = avg;
+    r->std = std::pow(sd / (A - 1), 0.5);
+    r->ps = (double)nmax / A;
+    r->best_agent = best;
+}
+
+int ensure_common(sbx_ctx *ctx, const SolveDims &d, int64_t total_steps)
+{
+    Work &w = ctx->w;
+    const size_t es = prec_bytes(d.prec);
+    const size_t nst = (size_t)d.n * d.Ap;
+    const size_t npl = (size_t)d.n * d.W;
+    CK(growv(w.x, w.cap_x, nst * es));
+    CK(growv(w.y, w.cap_y, nst * es));
+    CK(grow(w.S[0], w.cap_S0, npl));
+    CK(grow(w.S[1], w.cap_S1, npl));
+    CK(grow(w.Wp, w.cap_Wp, npl));
+    CK(grow(w.fin, w.cap_fin, npl));
+    CK(grow(w.chg, w.cap_chg, (size_t)d.W));
+    CK(grow(w.newmask, w.cap_new, (size_t)d.W));
+    CK(grow(w.stab, w.cap_stab, (size_t)d.Ap));
+    CK(grow(w.bif, w.cap_bif, (size_t)d.Ap));
+    CK(grow(w.prev, w.cap_prev, (size_t)d.Ap));
+    CK(grow(w.ctl, w.cap_ctl, (size_t)CTL_N));
+    CK(grow(w.eacc, w.cap_eacc, (size_t)d.Ap));
+    CK(grow(w.cut, w.cap_cut, (size_t)d.Ap));
+    const int64_t nwin = d.period > 0 ? total_steps / d.period + 2 : 2;
+    CK(grow(w.wincount, w.cap_win, (size_t)nwin));
+    CK(grow(w.coef32, w.cap_c32, (size_t)(total_steps + 2) * 4));
+    CK(grow(w.coef64, w.cap_c64, (size_t)(total_steps + 2) * 4));
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemsetAsync(w.Wp, 0xff, npl * 4, s));   // current_spins = -1 (ising.cu:128)
+    CK(cudaMemsetAsync(w.fin, 0xff, npl * 4, s));  // final_spins = -1 (ising.cu:129)
+    CK(cudaMemsetAsync(w.S[0], 0, npl * 4, s));
+    CK(cudaMemsetAsync(w.S[1], 0, npl * 4, s));
+    CK(cudaMemsetAsync(w.chg, 0, (size_t)d.W * 4, s));
+    CK(cudaMemsetAsync(w.newmask, 0, (size_t)d.W * 4, s));
+    CK(cudaMemsetAsync(w.stab, 0, (size_t)d.Ap * 4, s));
+    CK(cudaMemsetAsync(w.bif, 0, (size_t)d.Ap, s));
+    CK(cudaMemsetAsync(w.prev, 0, (size_t)d.Ap, s));
+    CK(cudaMemsetAsync(w.ctl, 0, CTL_N * 4, s));
+    CK(cudaMemsetAsync(w.wincount, 0, (size_t)nwin * 4, s));
+    return SBX_OK;
+}
+
+int init_state(sbx_ctx *ctx, const SolveDims &d, uint32_t seed, bool tsp)
+{
+    const int64_t outputs = d.n * d.A * (tsp ? 1 : 2);
+    const int64_t L = 31 * 32;
+    const int nbits = rand_threads_bits(outputs, L);
+    std::vector<uint32_t> tab;
+    rand_jump_tables(seed, L, nbits, tab);
+    CK(grow(ctx->w.rjump, ctx->w.cap_rj, tab.size()));
+    CK(cudaMemcpyAsync(ctx->w.rjump, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(launch_rand_init(d, ctx->w, tsp, L, nbits, ctx->stream));
+    // the table must outlive the async copy
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SBX_OK;
+}
+
+int upload_coef(sbx_ctx *ctx, const SolveDims &d, int64_t total_steps)
+{
+    std::vector<float> c32((size_t)(total_steps + 2) * 4);
+    std::vector<double> c64((size_t)(total_steps + 2) * 4);
+    for (int64_t k = 0; k < total_steps + 2; k++) {
+        const double p = 1.025 * (double)k / d.steps;    // kernels.cu:15 / :225
+        const double pc = p < 1.0 ? p : 1.0;
+        const double v[4] = {d.dt * (pc + 1), d.dt * (pc - 1), d.dt * (p + 1), d.dt * (p - 1)};
+        for (int j = 0; j < 4; j++) {
+            c64[k * 4 + j] = v[j];
+            c32[k * 4 + j] = (float)v[j];
+        }
+    }
+    CK(cudaMemcpyAsync(ctx->w.coef32, c32.data(), c32.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->w.coef64, c64.data(), c64.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SBX_OK;
+}
+
+bool poll_stop(sbx_ctx *ctx, int64_t c, bool force_all)
+{
+    // Enqueue a read of the stop flag after chunk c; wait for the one issued
+    // three chunks earlier.  At most three chunks run past the exit.
+    const int slot = (int)(c & 3);
+    cudaMemcpyAsync(&ctx->pinned[slot], ctx->w.ctl + CTL_STOP, 4, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaEventRecord(ctx->evp[slot], ctx->stream);
+    const int64_t old = force_all ? c : c - 3;
+    if (old < 0) return false;
+    cudaEventSynchronize(ctx->evp[old & 3]);
+    return ctx->pinned[old & 3] != 0;
+}
+
+int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_result *res,
+                 double *agent_values)
+{
+    SolveDims d;
+    d.n = p->J.n;
+    d.A = pr->agents;
+    d.Ap = (pr->agents + 31) / 32 * 32;
+    d.W = d.Ap / 32;
+    d.prec = pr->precision;
+    d.steps = pr->steps;
+    d.period = pr->period > 0 ? pr->period : 100;       // csr.cuh:109
+    d.threshold = pr->threshold > 0 ? pr->threshold : 25; // csr.cuh:108
+    d.fused = pr->fused ? 1 : 0;
+    d.uw = pr->update_window ? 1 : 0;
+    d.dt = pr->dt;
+    d.xi0 = xi0_of(p->J);
+    d.c0 = d.dt * d.xi0;
+    d.pdl = !(pr->flags & SBX_FLAG_NO_PDL);
+    const bool profile = (pr->flags & SBX_FLAG_PROFILE) != 0;
+    const bool use_graph = !(pr->flags & SBX_FLAG_NO_GRAPH) && !profile;
+    double kernel_ms = 0;
+    const int64_t nchunks = d.steps > 0 ? (d.steps + d.period - 1) / d.period : 0;
+    const int64_t total = nchunks * d.period;
+    cudaStream_t s = ctx->stream;
+    int rc = ensure_common(ctx, d, total);
+    if (rc) return rc;
+    if ((rc = upload_coef(ctx, d, total))) return rc;
+    if ((rc = init_state(ctx, d, pr->seed, false))) return rc;
+
+    int ka = 0;
+    if (pr->kernel != SBX_KERNEL_STREAM) ka = resident_pick_ka(d, p->J, pr->agents_per_block);
+    if (pr->kernel == SBX_KERNEL_RESIDENT && !ka)
+        return fail(ctx, SBX_ERR_UNSUPPORTED, "resident kernel: shape does not fit on chip (or FP64)");
+    int launches = 0, hot = 0;
+    CK(cudaEventRecord(ctx->ev0, s));
+    if (ka) {
+        if (d.uw) {
+            for (int64_t c = 0; c < std::max<int64_t>(nchunks, 1); c++) {
+                CK(launch_resident(d, p->J, ctx->w, ka, (int32_t)(c * d.period),
+                                   nchunks ? d.period : 0, c == 0, s));
+                launches++;
+                hot++;
+                if (poll_stop(ctx, c, false)) break;
+            }
+        } else {
+            CK(launch_resident(d, p->J, ctx->w, ka, 0, (int32_t)total, true, s));
+            launches++;
+            hot++;
+        }
+    } else {
+        CK(launch_prestep(d, p->J, ctx->w, s, &launches));
+        if (nchunks) {
+            int per_chunk = 0;
+            if (use_graph) {
+                char key[256];
+                snprintf(key, sizeof key, "%p/%lld/%d/%d/%d/%d/%d/%d/%d/%d/%.17g/%llu/%p", (void *)p,
+                         (long long)d.n, d.A, d.prec, d.period, d.fused, d.uw, d.threshold, (int)d.pdl,
+                         d.steps, d.c0, (unsigned long long)g_alloc_gen, (void *)s);
+                if (!ctx->gexec || ctx->gkey != key) {
+                    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+                    ctx->gexec = nullptr;
+                    cudaGraph_t g;
+                    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                    cudaError_t e = launch_chunk(d, p->J, ctx->w, s, &per_chunk);
+                    cudaError_t e2 = cudaStreamEndCapture(s, &g);
+                    CK(e);
+                    CK(e2);
+                    CK(cudaGraphInstantiate(&ctx->gexec, g, 0));
+                    cudaGraphDestroy(g);
+                    ctx->gkey = key;
+                } else {
+                    per_chunk = d.fused ? d.period + 2 : d.period + 3;
+                }
+                for (int64_t c = 0; c < nchunks; c++) {
+                    CK(cudaGraphLaunch(ctx->gexec, s));
+                    launches += per_chunk;
+                    if (d.uw && poll_stop(ctx, c, false)) break;
+                }
+            } else {
+                cudaEvent_t *evs = nullptr;
+                if (profile) {
+                    while ((int)ctx->prof.size() < 2 * d.period) {
+                        cudaEvent_t e;
+                        CK(cudaEventCreate(&e));
+                        ctx->prof.push_back(e);
+                    }
+                    evs = ctx->prof.data();
+                }
+                for (int64_t c = 0; c < nchunks; c++) {
+                    CK(launch_chunk(d, p->J, ctx->w, s, &launches, evs));
+                    if (profile) {
+                        CK(cudaStreamSynchronize(s));
+                        for (int i = 0; i < d.period; i++) {
+                            float t = 0;
+                            CK(cudaEventElapsedTime(&t, evs[2 * i], evs[2 * i + 1]));
+                            kernel_ms += t;
+                        }
+                    }
+                    if (d.uw && poll_stop(ctx, c, profile)) break;
+                }
+            }
+        }
+        hot = launches;
+    }
+    CK(cudaEventRecord(ctx->ev1, s));
+    const int loop_launches = launches;
+    CK(launch_cut(d, p->J, ctx->w, ctx->w.Wp, s, &launches));
+    std::vector<double> cut((size_t)d.A);
+    int32_t ctl[CTL_N];
+    std::vector<uint8_t> bif((size_t)d.A);
+    CK(cudaMemcpyAsync(cut.data(), ctx->w.cut, sizeof(double) * d.A, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ctl, ctx->w.ctl, sizeof ctl, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(bif.data(), ctx->w.bif, d.A, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    memset(res, 0, sizeof *res);
+    stats(cut, res);
+    res->time_us = ms * 1000.0;
+    res->xi0 = d.xi0;
+    res->steps_run = ctl[CTL_STEP];
+    res->windows_run = ctl[CTL_WINDOWS];
+    for (uint8_t b : bif) res->bifurcated += b;
+    res->kernel_used = ka ? SBX_KERNEL_RESIDENT : SBX_KERNEL_STREAM;
+    res->agents_per_block = ka;
+    if (ka) {
+        res->kernel_launches = hot;
+        res->kernel_ms = profile ? ms : 0;
+    } else {
+        // the step kernels: one per SB step actually run
+        res->kernel_launches = profile ? (int64_t)res->steps_run : loop_launches;
+        res->kernel_ms = kernel_ms;
+    }
+    res->gpu_launches = launches + 1;   // + the init kernel
+    if (agent_values) memcpy(agent_values, cut.data(), sizeof(double) * d.A);
+    ctx->have = true;
+    ctx->last_tsp = false;
+    ctx->d = d;
+    return SBX_OK;
+}
+
+int solve_tsp(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_result *res,
+              double *agent_values)
+{
+    const DevTsp &t = p->T;
+    SolveDims d;
+    d.n = (int64_t)t.N * t.N;
+    d.A = pr->agents;
+    d.Ap = (pr->agents + 31) / 32 * 32;
+    d.W = d.Ap / 32;
+    d.prec = pr->precision;
+    d.steps = pr->steps;
+    d.period = pr->period > 0 ? pr->period : pr->steps / 10;   // ising_tsp.cu:132
+    if (d.steps > 0 && d.period <= 0)
+        return fail(ctx, SBX_ERR_ARG, "TSP: 1..9 steps give a zero window period (the reference never ends)");
+    d.threshold = pr->threshold > 0 ? pr->threshold : 50;        // csr.cuh:167
+    d.dt = pr->dt;
+    d.xi0 = 0.002;                                               // ising_tsp.cu:61
+    d.c0 = d.dt * d.xi0;
+    d.pdl = !(pr->flags & SBX_FLAG_NO_PDL);
+    const int64_t nwin = d.period > 0 ? (d.steps + d.period - 1) / d.period : 1;
+    const int64_t total = d.period > 0 ? nwin * d.period : 0;
+    cudaStream_t s = ctx->stream;
+    int rc = ensure_common(ctx, d, total);
+    if (rc) return rc;
+    Work &w = ctx->w;
+    CK(grow(w.tours, w.cap_tours, (size_t)d.Ap * t.N));
+    CK(grow(w.valid, w.cap_valid, (size_t)d.Ap));
+    CK(cudaMemsetAsync(w.tours, 0xff, sizeof(int32_t) * d.Ap * t.N, s));
+    CK(cudaMemsetAsync(w.valid, 0, sizeof(int32_t) * d.Ap, s));
+    // schedules a(t), b(t) (kernels.cu:553-559), n = 2 (ising_tsp.cu:134)
+    std::vector<float> sch((size_t)(total + 1) * 2);
+    std::vector<double> ab((size_t)(total + 1) * 2);
+    for (int64_t k = 0; k <= total; k++) {
+        const int n2 = 2;
+        double a_t = n2 * 1.04 * (double)k / d.steps;
+        double b_t = 0.5 + ((double)0.5 * std::pow((double)k / (double)d.steps, 1.9));
+        a_t = a_t < n2 ? a_t : n2;
+        b_t = b_t < 1 ? b_t : 1;
+        ab[k * 2] = a_t;
+        ab[k * 2 + 1] = b_t;
+        sch[k * 2] = (float)b_t;
+        sch[k * 2 + 1] = (float)(d.dt * -(1 - a_t));
+    }
+    CK(grow(w.sched, w.cap_sched, (size_t)(total + 1)));
+    CK(grow(w.ab, w.cap_ab, (size_t)(total + 1)));
+    CK(cudaMemcpyAsync(w.sched, sch.data(), sch.size() * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(w.ab, ab.data(), ab.size() * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    if ((rc = init_state(ctx, d, pr->seed, true))) return rc;
+    int ka = 0;
+    if (pr->kernel != SBX_KERNEL_STREAM) ka = tsp_pick_ka(d, t, pr->agents_per_block);
+    if (pr->kernel == SBX_KERNEL_RESIDENT && !ka)
+        return fail(ctx, SBX_ERR_UNSUPPORTED, "TSP resident kernel: N > 32, FP64 or tile too wide");
+    if (!ka) {
+        CK(growv(w.x2, w.cap_x2, (size_t)d.n * d.Ap * prec_bytes(d.prec)));
+        CK(grow(w.visits, w.cap_visits, (size_t)2 * t.N * d.Ap));
+        CK(cudaMemsetAsync(w.visits, 0, sizeof(int32_t) * 2 * t.N * d.Ap, s));
+    }
+    int launches = 0, hot = 0;
+    CK(cudaEventRecord(ctx->ev0, s));
+    if (ka) {
+        CK(launch_tsp_resident(d, t, w, ka, s));
+        launches = hot = 1;
+    } else {
+        CK(launch_tsp_stream(d, t, w, s, &launches));
+        hot = launches;
+        int32_t c2[2] = {(int32_t)total, (int32_t)nwin};
+        CK(cudaMemcpyAsync(w.ctl, c2, sizeof c2, cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaEventRecord(ctx->ev1, s));
+    std::vector<int32_t> tours((size_t)d.A * t.N), valid((size_t)d.A);
+    std::vector<uint8_t> bif((size_t)d.A);
+    int32_t ctl[CTL_N];
+    CK(cudaMemcpyAsync(tours.data(), w.tours, tours.size() * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(valid.data(), w.valid, valid.size() * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(bif.data(), w.bif, d.A, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ctl, w.ctl, sizeof ctl, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    // Decode and statistics, src/ising_tsp.cu:188-239 and :272-287.
+    memset(res, 0, sizeof *res);
+    std::vector<double> all;
+    double total_len = 0, mn = DBL_MAX, mx = -DBL_MAX;
+    int32_t best = -1;
+    const int N = t.N;
+    for (int32_t a = 0; a < d.A; a++) {
+        double len = NAN;
+        if (valid[a] > 0) {
+            len = 0.0;
+            for (int i = 0; i < N; i++) {
+                const int c1 = std::min(tours[(size_t)a * N + i], tours[(size_t)a * N + (i + 1) % N]);
+                const int c2 = std::max(tours[(size_t)a * N + i], tours[(size_t)a * N + (i + 1) % N]);
+                len += t.packed[(size_t)(c2 + c1 * N - (c1 + 2) * (c1 + 1) / 2)];
+            }
+            all.push_back(len);
+            total_len += len;
+            if (len < mn) {
+                mn = len;
+                best = a;
+            }
+            if (len > mx) mx = len;
+        }
+        if (agent_values) agent_values[a] = len;
+    }
+    const int64_t nv = (int64_t)all.size();
+    const double avg = total_len / nv;
+    double sd = 0;
+    for (double v : all) sd += std::pow(v - avg, 2);
+    sd = std::pow(sd / (nv - 1), 0.5);
+    res->min = mn;
+    res->max = mx;
+    res->mean = avg;
+    res->std = sd;
+    res->valid = nv;
+    res->best_agent = best;
+    res->time_us = ms * 1000.0;
+    res->xi0 = d.xi0;
+    res->steps_run = ctl[CTL_STEP];
+    res->windows_run = ctl[CTL_WINDOWS];
+    for (uint8_t b : bif) res->bifurcated += b;
+    res->kernel_used = ka ? SBX_KERNEL_RESIDENT : SBX_KERNEL_STREAM;
+    res->agents_per_block = ka;
+    res->kernel_launches = hot;
+    res->gpu_launches = launches + 1;
+    ctx->have = true;
+    ctx->last_tsp = true;
+    ctx->d = d;
+    ctx->N = N;
+    return SBX_OK;
+}
+
+float bf16_to_f(uint16_t h)
+{
+    uint32_t u = (uint32_t)h << 16;
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
+float f16_to_f(uint16_t h)
+{
+    const uint32_t sign = (uint32_t)(h >> 15) << 31;
+    uint32_t ex = (h >> 10) & 0x1f, man = h & 0x3ff, u;
+    if (ex == 0) {
+        if (man == 0) u = sign;
+        else {   // subnormal
+            ex = 127 - 15 + 1;
+            while (!(man & 0x400)) {
+                man <<= 1;
+                ex--;
+            }
+            man &= 0x3ff;
+            u = sign | (ex << 23) | (man << 13);
+        }
+    } else if (ex == 31) {
+        u = sign | 0x7f800000u | (man << 13);
+    } else {
+        u = sign | ((ex + 127 - 15) << 23) | (man << 13);
+    }
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *sbx_strerror(int status)
+{
+    switch (status) {
+    case SBX_OK: return "ok";
+    case SBX_ERR_ARG: return "invalid argument";
+    case SBX_ERR_CUDA: return "CUDA runtime error";
+    case SBX_ERR_NOMEM: return "out of memory";
+    case SBX_ERR_IO: return "cannot open or read file";
+    case SBX_ERR_FORMAT: return "malformed input file";
+    case SBX_ERR_UNSUPPORTED: return "unsupported request";
+    case SBX_ERR_NODEVICE: return "no usable CUDA device";
+    case SBX_ERR_STATE: return "no solve to read back";
+    default: return "unknown status";
+    }
+}
+
+const char *sbx_version(void) { return "sbx 0.1 (sm_103a)"; }
+
+const char *sbx_last_error(void) { return g_err.c_str(); }
+
+void sbx_params_default(sbx_params *p)
+{
+    memset(p, 0, sizeof *p);
+    p->dt = 0.1;
+    p->steps = 10000;
+    p->agents = 1024;
+    p->fused = 1;
+    p->precision = SBX_F32;
+    p->seed = 1;
+}
+
+int sbx_create(sbx_ctx **out, int device)
+{
+    sbx_ctx *ctx = nullptr;
+    if (!out) return fail(ctx, SBX_ERR_ARG, "null ctx pointer");
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0 || device < 0 || device >= n)
+        return fail(ctx, SBX_ERR_NODEVICE, "no CUDA device");
+    ctx = new sbx_ctx;
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+    for (int i = 0; i < 4 && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&ctx->evp[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->pinned, 16);
+    if (e != cudaSuccess) {
+        sbx_destroy(ctx);
+        return fail(nullptr, SBX_ERR_CUDA, std::string("sbx_create: ") + cudaGetErrorString(e));
+    }
+    ctx->stream = ctx->own;
+    *out = ctx;
+    return SBX_OK;
+}
+
+int sbx_destroy(sbx_ctx *ctx)
+{
+    if (!ctx) return SBX_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    Work &w = ctx->w;
+    void *ptrs[] = {w.x, w.y, w.x2, w.S[0], w.S[1], w.Wp, w.fin, w.chg, w.newmask, w.stab, w.bif,
+                    w.prev, w.ctl, w.wincount, w.visits, w.ab, w.sched, w.eacc, w.cut, w.trace,
+                    w.tours, w.valid, w.rjump, w.coef32, w.coef64};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    for (auto &e : ctx->evp)
+        if (e) cudaEventDestroy(e);
+    for (auto &e : ctx->prof) cudaEventDestroy(e);
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->own) cudaStreamDestroy(ctx->own);
+    delete ctx;
+    return SBX_OK;
+}
+
+int sbx_set_stream(sbx_ctx *ctx, void *stream)
+{
+    if (!ctx) return SBX_ERR_ARG;
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own;
+    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    ctx->gexec = nullptr;
+    ctx->gkey.clear();
+    return SBX_OK;
+}
+
+int sbx_problem_csr(sbx_ctx *ctx, int64_t n, int64_t nnz, const int32_t *rowptr,
+                    const int32_t *col, const double *val, double weight_sum, sbx_problem **out)
+{
+    if (!ctx || !out) return fail(ctx, SBX_ERR_ARG, "null argument");
+    CK(cudaSetDevice(ctx->device));
+    sbx_problem *p = new sbx_problem;
+    p->ctx = ctx;
+    int rc = upload_csr(ctx, p->J, n, nnz, rowptr, col, val, weight_sum);
+    if (rc) {
+        free_csr(p->J);
+        delete p;
+        return rc;
+    }
+    *out = p;
+    return SBX_OK;
+}
+
+int sbx_problem_tsp(sbx_ctx *ctx, int32_t N, const double *packed, double A, double B, double C,
+                    sbx_problem **out)
+{
+    if (!ctx || !out || !packed) return fail(ctx, SBX_ERR_ARG, "null argument");
+    if (N < 2 || N > 4096) return fail(ctx, SBX_ERR_ARG, "TSP: need 2 <= N <= 4096 cities");
+    CK(cudaSetDevice(ctx->device));
+    sbx_problem *p = new sbx_problem;
+    p->ctx = ctx;
+    p->tsp = true;
+    DevTsp &t = p->T;
+    t.N = N;
+    t.A = A;
+    t.B = B;
+    t.C = C;
+    const int64_t nd = (int64_t)N * (N - 1) / 2;
+    t.packed.assign(packed, packed + nd);
+    // per-city sums in the reference's walk order (tsp_gpu.cu:51-68)
+    t.rowsum.assign(N, 0.0);
+    {
+        int i = 0, j = 0;
+        for (int64_t k = 0; k < nd; k++) {
+            if (j == N - 1) {
+                i++;
+                j = i;
+            }
+            j++;
+            t.rowsum[i] += packed[k];
+            t.rowsum[j] += packed[k];
+        }
+    }
+    auto pidx = [&](int c1, int c2) { return (int64_t)c2 + (int64_t)c1 * N - (int64_t)(c1 + 2) * (c1 + 1) / 2; };
+    std::vector<float> D((size_t)N * N, 0.f);
+    for (int k = 0; k < N; k++)
+        for (int l = 0; l < N; l++)
+            if (k != l) D[(size_t)k * N + l] = (float)packed[pidx(std::min(k, l), std::max(k, l))];
+    t.I2h.resize(N);
+    std::vector<float> I2f(N);
+    for (int c = 0; c < N; c++) {   // kernels.cu:591-592
+        t.I2h[c] = -1 * (A * t.rowsum[c] + (N - 2) * (B + C)) / 2;
+        I2f[c] = (float)t.I2h[c];
+    }
+    int rc = SBX_OK;
+    cudaError_t e = cudaMalloc(&t.D, sizeof(float) * N * N);
+    if (e == cudaSuccess) e = cudaMalloc(&t.I2, sizeof(float) * N);
+    if (e == cudaSuccess) e = cudaMalloc(&t.I2d, sizeof(double) * N);
+    if (e == cudaSuccess) e = cudaMemcpy(t.D, D.data(), sizeof(float) * N * N, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(t.I2, I2f.data(), sizeof(float) * N, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(t.I2d, t.I2h.data(), sizeof(double) * N, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) rc = fail(ctx, SBX_ERR_CUDA, cudaGetErrorString(e));
+    // The QUBO as CSR, tsp_gpu.cu:76-112 then CSR::from_matrix (row-major
+    // nonzeros), for the streaming kernel.
+    if (!rc) {
+        const int64_t m = (int64_t)N * N;
+        std::vector<int32_t> rp(m + 1, 0), col;
+        std::vector<double> val;
+        for (int i = 0; i < N; i++)
+            for (int k = 0; k < N; k++) {
+                for (int j = 0; j < N; j++)
+                    for (int l = 0; l < N; l++) {
+                        double v;
+                        const bool adj = (i == j + 1 || j == i + 1 || (i == 0 && j == N - 1) ||
+                                          (i == N - 1 && j == 0));
+                        if (i != j && k == l) v = C / 4;
+                        else if (adj && k != l) {
+                            const int c1 = std::min(k, l), c2 = std::max(k, l);
+                            v = A * packed[((2 * (int64_t)N - c1 - 3) * c1) / 2 + c2 - 1] / 8;
+                        } else if (i == j && k != l) v = B / 4;
+                        else if (i == j && k == l) v = (B + C) / 4;
+                        else v = 0;
+                        if (v != 0) {
+                            col.push_back(j * N + l);
+                            val.push_back(v);
+                        }
+                    }
+                rp[(size_t)i * N + k + 1] = (int32_t)col.size();
+            }
+        rc = upload_csr(ctx, t.qubo, m, (int64_t)col.size(), rp.data(), col.data(), val.data(), 0.0);
+    }
+    if (rc) {
+        cudaFree(t.D);
+        cudaFree(t.I2);
+        cudaFree(t.I2d);
+        free_csr(t.qubo);
+        delete p;
+        return rc;
+    }
+    *out = p;
+    return SBX_OK;
+}
+
+int sbx_problem_destroy(sbx_problem *p)
+{
+    if (!p) return SBX_ERR_ARG;
+    if (p->ctx && p->ctx->gexec) {   // a cached graph may point at this problem
+        cudaGraphExecDestroy(p->ctx->gexec);
+        p->ctx->gexec = nullptr;
+        p->ctx->gkey.clear();
+    }
+    free_csr(p->J);
+    free_csr(p->T.qubo);
+    cudaFree(p->T.D);
+    cudaFree(p->T.I2);
+    cudaFree(p->T.I2d);
+    delete p;
+    return SBX_OK;
+}
+
+int sbx_problem_info(const sbx_problem *p, int64_t *n, int64_t *nnz, int32_t *is_tsp)
+{
+    if (!p) return SBX_ERR_ARG;
+    const DevCsr &J = p->tsp ? p->T.qubo : p->J;
+    if (n) *n = J.n;
+    if (nnz) *nnz = J.nnz;
+    if (is_tsp) *is_tsp = p->tsp;
+    return SBX_OK;
+}
+
+int sbx_solve(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_result *res,
+              double *agent_values)
+{
+    if (!ctx || !p || !pr || !res) return fail(ctx, SBX_ERR_ARG, "null argument");
+    if (pr->agents < 1 || pr->steps < 0 || !(pr->dt == pr->dt) || pr->precision < 0 || pr->precision > 3)
+        return fail(ctx, SBX_ERR_ARG, "bad params (agents >= 1, steps >= 0, precision 0..3)");
+    if (pr->agents < 2 && !p->tsp) {
+        // the reference's std dev divides by agents-1; one agent is allowed
+    }
+    const int64_t n = p->tsp ? (int64_t)p->T.N * p->T.N : p->J.n;
+    if ((double)n * ((pr->agents + 31) / 32 * 32) * 8.0 > 200e9)
+        return fail(ctx, SBX_ERR_NOMEM, "state larger than the device");
+    CK(cudaSetDevice(ctx->device));
+    ctx->have = false;
+    return p->tsp ? solve_tsp(ctx, p, pr, res, agent_values) : solve_maxcut(ctx, p, pr, res, agent_values);
+}
+
+int sbx_get_state(sbx_ctx *ctx, double *x, double *y, int32_t *spins)
+{
+    if (!ctx) return SBX_ERR_ARG;
+    if (!ctx->have) return fail(ctx, SBX_ERR_STATE, "no solve yet");
+    const SolveDims &d = ctx->d;
+    const size_t es = prec_bytes(d.prec), nst = (size_t)d.n * d.Ap;
+    std::vector<unsigned char> buf(nst * es);
+    for (int which = 0; which < 2; which++) {
+        double *out = which ? y : x;
+        if (!out) continue;
+        CK(cudaMemcpy(buf.data(), which ? ctx->w.y : ctx->w.x, nst * es, cudaMemcpyDeviceToHost));
+        for (int64_t r = 0; r < d.n; r++)
+            for (int a = 0; a < d.A; a++) {
+                const size_t i = (size_t)r * d.Ap + a;
+                double v;
+                if (d.prec == P_F64) memcpy(&v, &buf[i * 8], 8);
+                else if (d.prec == P_F32) {
+                    float f;
+                    memcpy(&f, &buf[i * 4], 4);
+                    v = f;
+                } else {
+                    uint16_t h;
+                    memcpy(&h, &buf[i * 2], 2);
+                    v = d.prec == P_BF16 ? bf16_to_f(h) : f16_to_f(h);
+                }
+                out[(size_t)r * d.A + a] = v;
+            }
+    }
+    if (spins) {
+        std::vector<uint32_t> pl((size_t)d.n * d.W);
+        CK(cudaMemcpy(pl.data(), ctx->w.Wp, pl.size() * 4, cudaMemcpyDeviceToHost));
+        for (int64_t r = 0; r < d.n; r++)
+            for (int a = 0; a < d.A; a++)
+                spins[(size_t)r * d.A + a] = ((pl[(size_t)r * d.W + a / 32] >> (a % 32)) & 1u) ? -1 : 1;
+    }
+    return SBX_OK;
+}
+
+int sbx_get_tours(sbx_ctx *ctx, int32_t *tours, int32_t *valid_step)
+{
+    if (!ctx) return SBX_ERR_ARG;
+    if (!ctx->have || !ctx->last_tsp) return fail(ctx, SBX_ERR_STATE, "no TSP solve yet");
+    const int A = ctx->d.A, N = ctx->N;
+    std::vector<int32_t> v((size_t)A);
+    CK(cudaMemcpy(v.data(), ctx->w.valid, sizeof(int32_t) * A, cudaMemcpyDeviceToHost));
+    if (valid_step) memcpy(valid_step, v.data(), sizeof(int32_t) * A);
+    if (tours) {
+        CK(cudaMemcpy(tours, ctx->w.tours, sizeof(int32_t) * A * N, cudaMemcpyDeviceToHost));
+        for (int a = 0; a < A; a++)
+            if (v[a] <= 0)
+                for (int i = 0; i < N; i++) tours[(size_t)a * N + i] = -1;
+    }
+    return SBX_OK;
+}
+
+int sbx_solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const int32_t *agents,
+                    const sbx_params *params, sbx_result *res, double *agent_values, double *batch_time_us)
+{
+    (void)count;
+    (void)problems;
+    (void)agents;
+    (void)params;
+    (void)res;
+    (void)agent_values;
+    (void)batch_time_us;
+    return fail(ctx, SBX_ERR_UNSUPPORTED, "batched solve not built yet");
+}
+
+int sbx_get_trace(sbx_ctx *ctx, int64_t cap, int64_t *steps, double *best, int64_t *count)
+{
+    (void)cap;
+    (void)steps;
+    (void)best;
+    if (!ctx) return SBX_ERR_ARG;
+    if (count) *count = 0;
+    return fail(ctx, SBX_ERR_UNSUPPORTED, "trace not recorded");
+}
+
+}  // extern "C"

@@ -1,0 +1,115 @@
+// engine.h -- internal interface between the C-ABI host layer (api.cpp) and
+// the CUDA launchers (k_*.cu).  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+namespace sbx {
+
+enum Prec { P_F32 = 0, P_BF16 = 1, P_F16 = 2, P_F64 = 3 };
+
+inline size_t prec_bytes(int p) { return p == P_F64 ? 8 : p == P_F32 ? 4 : 2; }
+
+// MaxCut / QUBO matrix on the device.  colw holds the column index; when every
+// weight is +-1 ("unit"), bit 31 holds the weight's sign and no value array is
+// read by the step kernels.
+struct DevCsr {
+    int64_t n = 0, nnz = 0;
+    int32_t *rowptr = nullptr;
+    uint32_t *colw = nullptr;
+    double *vald = nullptr;
+    float *valf = nullptr;
+    int32_t *perm = nullptr; // rows in decreasing degree (resident kernel order)
+    bool unit = false;       // all |w| == 1
+    bool integer = false;    // all integer-valued, small enough for int32 sums
+    double wsum = 0;         // reference csr.sum
+    int32_t max_deg = 0;
+    std::vector<double> hval;   // host copy of values (xi0)
+    std::vector<int32_t> hrowptr, hcol;
+};
+
+// Control words shared by the kernels of one solve.
+enum Ctl { CTL_STEP = 0, CTL_STOP = 1, CTL_WINDOWS = 2, CTL_NBIF = 3, CTL_N = 8 };
+
+// Device buffers of one solve (grown on demand, owned by the context).
+struct Work {
+    void *x = nullptr, *y = nullptr, *x2 = nullptr;
+    uint32_t *S[2] = {nullptr, nullptr};
+    uint32_t *Wp = nullptr, *fin = nullptr, *chg = nullptr, *newmask = nullptr;
+    int32_t *stab = nullptr;
+    uint8_t *bif = nullptr, *prev = nullptr;
+    int32_t *ctl = nullptr;
+    int32_t *wincount = nullptr;          // bifurcated agents after each window
+    int32_t *visits = nullptr;            // TSP streaming window scratch
+    double2 *ab = nullptr;                // TSP (a_t, b_t) per step, FP64
+    float2 *sched = nullptr;              // TSP (b_t, dt*-(1-a_t)) per step
+    unsigned long long *eacc = nullptr;   // per-agent cut accumulators
+    double *cut = nullptr;                // per-agent cuts
+    double *trace = nullptr;              // per-window best cut
+    int32_t *tours = nullptr, *valid = nullptr;
+    uint32_t *rjump = nullptr;            // rand jump tables
+    float *coef32 = nullptr;              // per-step coefficients (float4 / step)
+    double *coef64 = nullptr;             // the same in FP64 (double4 / step)
+    size_t cap_x = 0, cap_y = 0, cap_x2 = 0, cap_S0 = 0, cap_S1 = 0, cap_Wp = 0, cap_fin = 0,
+           cap_chg = 0, cap_new = 0, cap_stab = 0, cap_bif = 0, cap_prev = 0, cap_ctl = 0,
+           cap_win = 0, cap_visits = 0, cap_ab = 0, cap_sched = 0, cap_eacc = 0, cap_cut = 0,
+           cap_trace = 0, cap_tours = 0, cap_valid = 0, cap_rj = 0, cap_c32 = 0, cap_c64 = 0;
+};
+
+// One solve's shape and scalars.
+struct SolveDims {
+    int64_t n = 0;
+    int32_t A = 0, Ap = 0, W = 0;
+    int prec = P_F32;
+    int32_t steps = 0, period = 100, threshold = 25;
+    int fused = 1, uw = 0;
+    double dt = 0.1, xi0 = 0, c0 = 0;
+    bool pdl = true;
+};
+
+// ---- launchers (k_*.cu) ----
+
+// glibc rand() jump tables for `seed`: V0 (31 words) + nbits matrices of
+// 31x31, each M^(L*2^b).  Returns the words in `out`.
+void rand_jump_tables(uint32_t seed, int64_t L, int nbits, std::vector<uint32_t> &out);
+int rand_threads_bits(int64_t outputs, int64_t L);
+// x, y <- the reference's init stream (tsp: x = 0, y from the stream).
+cudaError_t launch_rand_init(const SolveDims &d, Work &w, bool tsp, int64_t L, int nbits,
+                             cudaStream_t s);
+
+// Streaming MaxCut kernels (k_stream.cu).
+cudaError_t launch_prestep(const SolveDims &d, const DevCsr &J, Work &w, cudaStream_t s,
+                           int *launches);
+// evs (optional): 2*period events recorded around each step kernel.
+cudaError_t launch_chunk(const SolveDims &d, const DevCsr &J, Work &w, cudaStream_t s,
+                         int *launches, cudaEvent_t *evs = nullptr);
+cudaError_t launch_cut(const SolveDims &d, const DevCsr &J, Work &w, const uint32_t *plane,
+                       cudaStream_t s, int *launches);
+
+// Resident MaxCut kernel (k_resident.cu): returns cudaErrorInvalidValue when the
+// shape does not fit.
+int resident_pick_ka(const SolveDims &d, const DevCsr &J, int requested);
+size_t resident_smem_bytes(const SolveDims &d, int ka);
+cudaError_t launch_resident(const SolveDims &d, const DevCsr &J, Work &w, int ka,
+                            int32_t step0, int32_t nsteps, bool first, cudaStream_t s);
+
+// TSP kernels (k_tsp.cu).
+struct DevTsp {
+    int32_t N = 0;
+    double A = 1, B = 0, C = 0;
+    std::vector<double> packed, rowsum, I2h;   // host
+    float *D = nullptr;                   // device N x N distances (float)
+    float *I2 = nullptr;                  // device per-city linear field (float)
+    double *I2d = nullptr;                // the same in FP64
+    DevCsr qubo;                          // the QUBO as CSR (streaming path)
+};
+int tsp_pick_ka(const SolveDims &d, const DevTsp &t, int requested);
+cudaError_t launch_tsp_resident(const SolveDims &d, const DevTsp &t, Work &w, int ka,
+                                cudaStream_t s);
+cudaError_t launch_tsp_stream(const SolveDims &d, const DevTsp &t, Work &w, cudaStream_t s,
+                              int *launches);
+
+}  // namespace sbx
