@@ -67,6 +67,8 @@ typedef struct sbx_params {
     int32_t agents_per_block; /* resident kernel tile; 0: autotuned */
     int32_t trace;          /* 1: record the best cut at every window */
     uint32_t flags;         /* SBX_FLAG_* */
+    int32_t run_steps;      /* run only the first run_steps steps of the
+                               schedule set by `steps` (0: all of them) */
 } sbx_params;
 
 typedef struct sbx_result {

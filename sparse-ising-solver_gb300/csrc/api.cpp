@@ -323,7 +323,8 @@ int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_r
     const bool profile = (pr->flags & SBX_FLAG_PROFILE) != 0;
     const bool use_graph = !(pr->flags & SBX_FLAG_NO_GRAPH) && !profile;
     double kernel_ms = 0;
-    const int64_t nchunks = d.steps > 0 ? (d.steps + d.period - 1) / d.period : 0;
+    const int32_t run = pr->run_steps > 0 ? std::min(pr->run_steps, pr->steps) : pr->steps;
+    const int64_t nchunks = run > 0 ? (run + d.period - 1) / d.period : 0;
     const int64_t total = nchunks * d.period;
     cudaStream_t s = ctx->stream;
     int rc = ensure_common(ctx, d, total);
@@ -462,8 +463,10 @@ int solve_tsp(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
     d.xi0 = 0.002;                                               // ising_tsp.cu:61
     d.c0 = d.dt * d.xi0;
     d.pdl = !(pr->flags & SBX_FLAG_NO_PDL);
-    const int64_t nwin = d.period > 0 ? (d.steps + d.period - 1) / d.period : 1;
+    const int32_t run = pr->run_steps > 0 ? std::min(pr->run_steps, pr->steps) : pr->steps;
+    const int64_t nwin = d.period > 0 ? (run + d.period - 1) / d.period : 1;
     const int64_t total = d.period > 0 ? nwin * d.period : 0;
+    d.nwin = (int32_t)nwin;
     cudaStream_t s = ctx->stream;
     int rc = ensure_common(ctx, d, total);
     if (rc) return rc;
@@ -838,7 +841,8 @@ int sbx_solve(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
               double *agent_values)
 {
     if (!ctx || !p || !pr || !res) return fail(ctx, SBX_ERR_ARG, "null argument");
-    if (pr->agents < 1 || pr->steps < 0 || !(pr->dt == pr->dt) || pr->precision < 0 || pr->precision > 3)
+    if (pr->agents < 1 || pr->steps < 0 || !(pr->dt == pr->dt) || pr->precision < 0 ||
+        pr->precision > 3 || pr->run_steps < 0 || pr->period < 0 || pr->threshold < 0)
         return fail(ctx, SBX_ERR_ARG, "bad params (agents >= 1, steps >= 0, precision 0..3)");
     if (pr->agents < 2 && !p->tsp) {
         // the reference's std dev divides by agents-1; one agent is allowed

@@ -65,6 +65,7 @@ struct SolveDims {
     int32_t A = 0, Ap = 0, W = 0;
     int prec = P_F32;
     int32_t steps = 0, period = 100, threshold = 25;
+    int32_t nwin = 0;   // TSP: windows to run
     int fused = 1, uw = 0;
     double dt = 0.1, xi0 = 0, c0 = 0;
     bool pdl = true;

@@ -4,7 +4,7 @@
 // Layout.  x, y: [n][Ap] in the storage precision (Ap = agents rounded up to
 // 32).  Sign planes S[2], window plane Wp (the reference's current_spins),
 // final plane fin: [n][Ap/32] uint32, bit a%32 of word (r, a/32) = signbit of
-// x[r][a] (1 = spin -1).  A warp owns one (row, 32-agent word): lane = agent.
+// x[r][a] (1 = spin -1).
 //
 // Semantics (Jacobi): every gather of step k reads the sign plane written by
 // step k-1, so each step is the reference kernel run with all threads reading
@@ -14,6 +14,7 @@
 #include "common.cuh"
 #include "engine.h"
 
+#include <cstring>
 #include <type_traits>
 
 namespace sbx {
@@ -55,114 +56,198 @@ template <> struct Coef<double> {
     }
 };
 
-// -sum_j J_rj s_j for the 32 agents of word w (lane = agent), src/kernels.cu
-// :247-255.  Unit weights: count the negative products (sign bit XOR weight
-// sign) and return 2*count - degree, exact.  Other weights: the reference's
-// subtraction order over the row.
-template <int WM>
-__device__ __forceinline__ typename std::conditional<WM == W_F64, double, float>::type
-force(const StepP &P, int64_t r, int w, int lane, const uint32_t *__restrict__ Sin)
+__device__ __forceinline__ uint32_t spread4(uint32_t nib) { return (nib * 0x00204081u) & 0x01010101u; }
+
+// V consecutive storage elements moved as one naturally aligned vector.
+template <int B> struct Raw;
+template <> struct Raw<16> { uint4 u; };
+template <> struct Raw<8> { uint2 u; };
+template <> struct Raw<4> { uint32_t u; };
+template <> struct Raw<2> { unsigned short u; };
+template <class T, int V> __device__ __forceinline__ Raw<V * sizeof(T)> vload(const T *p)
 {
+    Raw<V * sizeof(T)> r;
+    r.u = *(const decltype(r.u) *)p;
+    return r;
+}
+template <class T, int V> __device__ __forceinline__ void unpack(const Raw<V * sizeof(T)> &r, T (&o)[V])
+{
+    memcpy(o, &r.u, V * sizeof(T));
+}
+template <class T, int V> __device__ __forceinline__ void vstore(T *p, const T (&o)[V])
+{
+    Raw<V * sizeof(T)> r;
+    memcpy(&r.u, o, V * sizeof(T));
+    *(decltype(r.u) *)p = r.u;
+}
+
+// One SB step over every (row, agent).  Work item = (row, segment of 32*V
+// agents); a warp takes items in turn, lane l owns V consecutive agents of the
+// segment (one vector load of x and of y).  Per neighbour j the lane reads the
+// sign word of its agents in row j of the plane (lanes of one word share the
+// address), XORs the weight's sign and adds the V bits into byte counters
+// (bit i of a nibble lands in byte i after multiplying by 0x00204081); the
+// force is 2*count - degree, exact (src/kernels.cu:247-255).  Byte counters
+// hold 7 chunks of 32 neighbours; BIG rows (degree > 224) flush them into ints.
+// The new signs of the V agents are OR-combined across the lanes of a word
+// and written once.
+template <class T, int V, int KIND, bool WIN, int WM, bool BIG>
+__global__ void __launch_bounds__(256) k_row(const StepP P, const int offset)
+{
+    using A = typename St<T>::A;
     using R = typename std::conditional<WM == W_F64, double, float>::type;
-    const int32_t e0 = __ldg(&P.rowptr[r]), e1 = __ldg(&P.rowptr[r + 1]);
-    int cnt = 0;
-    R tot = 0;
-    for (int32_t base = e0; base < e1; base += 32) {
-        const int m = min(32, e1 - base);
-        const uint32_t mycw = lane < m ? __ldg(&P.colw[base + lane]) : 0u;
-        R myv = 0;
-        if (WM == W_F32) myv = lane < m ? __ldg(&P.valf[base + lane]) : 0.f;
-        if (WM == W_F64) myv = lane < m ? __ldg(&P.vald[base + lane]) : 0.0;
-#pragma unroll 8
-        for (int k = 0; k < m; k++) {
-            const uint32_t cw = __shfl_sync(FULL, mycw, k);
-            const uint32_t word = __ldg(&Sin[(int64_t)(cw & 0x7fffffffu) * P.W + w]);
-            if (WM == W_UNIT) {
-                cnt += ((word >> lane) ^ (cw >> 31)) & 1u;
-            } else {
-                const R v = __shfl_sync(FULL, myv, k);
-                const R s = ((word >> lane) & 1u) ? R(-1) : R(1);
-                if (WM == W_F64) tot = sub(tot, mul(v, s));
-                else tot -= v * s;
+    extern __shared__ uint32_t s_chg[];   // [W] window steps: changed bits of this block
+    pdl_wait();
+    if (P.ctl[CTL_STOP]) return;          // block-uniform
+    const int step = P.ctl[CTL_STEP] + offset;
+    const int lane = threadIdx.x & 31;
+    if (WIN) {
+        for (int q = threadIdx.x; q < P.W; q += blockDim.x) s_chg[q] = 0;
+        __syncthreads();
+    }
+    pdl_trigger();
+    T *xp = (T *)P.x, *yp = (T *)P.y;
+    uint32_t *Scur = (step & 1) ? P.S1 : P.S0;
+    uint32_t *Snext = (step & 1) ? P.S0 : P.S1;
+    constexpr int G = 32 / V;   // lanes sharing one sign word
+    constexpr uint32_t VM = (V == 32) ? 0xffffffffu : ((1u << V) - 1u);
+    const int nit = P.Ap / (32 * V);
+    const int64_t items = P.n * nit;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t item = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); item < items;
+         item += nw) {
+        const int64_t r = item / nit;
+        const int it = (int)(item - r * nit);
+        const int a0 = it * 32 * V + lane * V;
+        const int q = a0 >> 5, off = a0 & 31;
+        const int64_t base = r * P.Ap + a0;
+        const auto xr = vload<T, V>(xp + base);
+        const auto yr = vload<T, V>(yp + base);
+        T xs[V], ys[V];
+        A x[V], y[V];
+        if (KIND == K_XY) {
+            // Update_XY, src/kernels.cu:8-22 (pressure not clamped)
+            const auto c = Coef<A>::get(P, step);
+            unpack<T, V>(xr, xs);
+            unpack<T, V>(yr, ys);
+#pragma unroll
+            for (int v = 0; v < V; v++) {
+                x[v] = St<T>::ld(xs[v]);
+                y[v] = St<T>::ld(ys[v]);
+                y[v] = add(y[v], mul((A)c.w, x[v]));
+                x[v] = add(x[v], mul((A)c.z, y[v]));
+            }
+        } else {
+            const int32_t e0 = __ldg(&P.rowptr[r]), e1 = __ldg(&P.rowptr[r + 1]);
+            const int deg = e1 - e0;
+            uint32_t lo = 0, hi = 0;
+            int cnt[BIG ? V : 1];
+            R tot[WM == W_UNIT ? 1 : V];
+#pragma unroll
+            for (int v = 0; v < (BIG ? V : 1); v++) cnt[v] = 0;
+#pragma unroll
+            for (int v = 0; v < (WM == W_UNIT ? 1 : V); v++) tot[v] = R(0);
+            int chunk = 0;
+            for (int32_t cb = e0; cb < e1; cb += 32, chunk++) {
+                const int m = min(32, e1 - cb);
+                const uint32_t mycw = lane < m ? __ldg(&P.colw[cb + lane]) : 0u;
+                R myv = R(0);
+                if (WM == W_F32) myv = lane < m ? __ldg(&P.valf[cb + lane]) : 0.f;
+                if (WM == W_F64) myv = lane < m ? __ldg(&P.vald[cb + lane]) : 0.0;
+#pragma unroll 4
+                for (int k = 0; k < m; k++) {
+                    const uint32_t cw = __shfl_sync(FULL, mycw, k);
+                    const uint32_t word = __ldg(&Scur[(int64_t)(cw & 0x7fffffffu) * P.W + q]);
+                    uint32_t bits = (word >> off) & VM;
+                    if (WM == W_UNIT) {
+                        bits ^= (0u - (cw >> 31)) & VM;
+                        lo += spread4(bits & 0xfu);
+                        if (V == 8) hi += spread4(bits >> 4);
+                    } else {
+                        const R wv = __shfl_sync(FULL, myv, k);
+#pragma unroll
+                        for (int v = 0; v < V; v++) {
+                            const R sv = ((bits >> v) & 1u) ? R(-1) : R(1);
+                            if (WM == W_F64) tot[v] = sub(tot[v], mul(wv, sv));
+                            else tot[v] -= wv * sv;
+                        }
+                    }
+                }
+                if (BIG && WM == W_UNIT && (chunk % 7 == 6 || cb + 32 >= e1)) {
+#pragma unroll
+                    for (int v = 0; v < (BIG ? V : 1); v++)
+                        cnt[v] += ((v < 4 ? lo : hi) >> (8 * (v & 3))) & 0xffu;
+                    lo = hi = 0;
+                }
+            }
+            const auto c = Coef<A>::get(P, step);
+            const A c0 = (A)P.c0;
+            unpack<T, V>(xr, xs);
+            unpack<T, V>(yr, ys);
+#pragma unroll
+            for (int v = 0; v < V; v++) {
+                x[v] = St<T>::ld(xs[v]);
+                y[v] = St<T>::ld(ys[v]);
+                int cv;
+                if (BIG) cv = cnt[v < (BIG ? V : 1) ? v : 0];
+                else cv = ((v < 4 ? lo : hi) >> (8 * (v & 3))) & 0xffu;
+                const A total = (WM == W_UNIT) ? (A)(2 * cv - deg) : (A)tot[WM == W_UNIT ? 0 : v];
+                if (KIND == K_FUSED) {
+                    // src/kernels.cu:236-262: clamp or kick, then the drift /
+                    // kick pair that runs unconditionally (a clamped oscillator
+                    // leaves with y = dt (p-1) sign(x)).
+                    if (fabs(x[v]) > A(1)) {
+                        x[v] = spin_of(x[v]);
+                        y[v] = A(0);
+                    } else {
+                        y[v] = add(y[v], mul(c0, total));
+                    }
+                    x[v] = add(x[v], mul((A)c.x, y[v]));
+                    y[v] = add(y[v], mul((A)c.y, x[v]));
+                } else {
+                    // mat_mult (:207) and confine (:158-165) of this step, then
+                    // Update_XY of the next one unless the window closes here.
+                    y[v] = add(y[v], mul(c0, total));
+                    if (fabs(x[v]) > A(1)) {
+                        x[v] = spin_of(x[v]);
+                        y[v] = A(0);
+                    }
+                    if (!WIN) {
+                        const auto cn = Coef<A>::get(P, step + 1);
+                        y[v] = add(y[v], mul((A)cn.w, x[v]));
+                        x[v] = add(x[v], mul((A)cn.z, y[v]));
+                    }
+                }
+            }
+        }
+        uint32_t b = 0;
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+            xs[v] = St<T>::st(x[v]);
+            ys[v] = St<T>::st(y[v]);
+            b |= sbit(St<T>::ld(xs[v])) << v;
+        }
+        vstore<T, V>(xp + base, xs);
+        vstore<T, V>(yp + base, ys);
+        b <<= off;
+#pragma unroll
+        for (int sft = 1; sft < G; sft <<= 1) b |= __shfl_xor_sync(FULL, b, sft);
+        if ((lane & (G - 1)) == 0) {
+            const int64_t wi = r * P.W + q;
+            if (KIND == K_XY) Scur[wi] = b;
+            else if (KIND == K_FUSED || !WIN) Snext[wi] = b;
+            if (WIN) {
+                // window compare, src/kernels.cu:37-46 + :84-90
+                const uint32_t ch = b ^ P.Wp[wi];
+                P.Wp[wi] = b;
+                if (ch) atomicOr(&s_chg[q], ch);
             }
         }
     }
-    if (WM == W_UNIT) return (R)(2 * cnt - (e1 - e0));
-    return tot;
-}
-
-template <class T, int KIND, bool WIN, int WM>
-__global__ void __launch_bounds__(256) k_step(const StepP P, const int offset)
-{
-    using A = typename St<T>::A;
-    pdl_wait();
-    if (P.ctl[CTL_STOP]) return;
-    const int step = P.ctl[CTL_STEP] + offset;
-    const int64_t gw = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    pdl_trigger();
-    if (gw >= P.n * P.W) return;
-    const int64_t r = gw / P.W;
-    const int w = (int)(gw - r * P.W);
-    const int64_t idx = r * P.Ap + (int64_t)w * 32 + lane;
-    T *xp = (T *)P.x, *yp = (T *)P.y;
-    A x = St<T>::ld(xp[idx]), y = St<T>::ld(yp[idx]);
-    uint32_t *Sin = (step & 1) ? P.S1 : P.S0;
-    uint32_t *Snext = (step & 1) ? P.S0 : P.S1;
-    const int64_t wi = r * P.W + w;
-
-    if (KIND == K_XY) {
-        // Update_XY, src/kernels.cu:8-22 (pressure not clamped); writes the
-        // plane that step `step` gathers from.
-        const auto c = Coef<A>::get(P, step);
-        y = add(y, mul((A)c.w, x));
-        x = add(x, mul((A)c.z, y));
-        xp[idx] = St<T>::st(x);
-        yp[idx] = St<T>::st(y);
-        const uint32_t b = __ballot_sync(FULL, sbit(x));
-        if (lane == 0) Sin[wi] = b;
-        return;
-    }
-
-    const A total = (A)force<WM>(P, r, w, lane, Sin);
-    if (KIND == K_FUSED) {
-        // src/kernels.cu:236-262: clamp or kick, then the drift/kick pair that
-        // runs unconditionally (so a clamped oscillator leaves with
-        // y = dt (p-1) sign(x)).
-        const auto c = Coef<A>::get(P, step);
-        if (fabs(x) > A(1)) {
-            x = spin_of(x);
-            y = A(0);
-        } else {
-            y = add(y, mul((A)P.c0, total));
-        }
-        x = add(x, mul((A)c.x, y));
-        y = add(y, mul((A)c.y, x));
-    } else {
-        // K_FC: mat_mult (:207) then confine (:158-165) of step `step`; then,
-        // unless the window closes here, Update_XY of step+1.
-        y = add(y, mul((A)P.c0, total));
-        if (fabs(x) > A(1)) {
-            x = spin_of(x);
-            y = A(0);
-        }
-        if (!WIN) {
-            const auto c = Coef<A>::get(P, step + 1);
-            y = add(y, mul((A)c.w, x));
-            x = add(x, mul((A)c.z, y));
-        }
-    }
-    xp[idx] = St<T>::st(x);
-    yp[idx] = St<T>::st(y);
-    const uint32_t b = __ballot_sync(FULL, sbit(x));
-    if (lane == 0) {
-        if (KIND == K_FUSED || !WIN) Snext[wi] = b;
-        if (WIN) {
-            // window compare, src/kernels.cu:37-46 + :84-90
-            const uint32_t ch = b ^ P.Wp[wi];
-            if (ch) atomicOr(&P.chg[w], ch);
-            P.Wp[wi] = b;
-        }
+    if (WIN) {
+        __syncthreads();
+        for (int qq = threadIdx.x; qq < P.W; qq += blockDim.x)
+            if (s_chg[qq]) atomicOr(&P.chg[qq], s_chg[qq]);
     }
 }
 
@@ -228,12 +313,12 @@ __global__ void __launch_bounds__(256) k_win_snap(const WinP P)
 }
 
 template <class K, class... Args>
-cudaError_t launch(K kern, dim3 grid, dim3 block, cudaStream_t s, bool pdl, Args... args)
+cudaError_t launch(K kern, dim3 grid, dim3 block, size_t smem, cudaStream_t s, bool pdl, Args... args)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
     cfg.blockDim = block;
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -266,27 +351,73 @@ StepP make_step(const SolveDims &d, const DevCsr &J, Work &w)
     return P;
 }
 
-template <class T, int KIND, bool WIN>
-cudaError_t step_wm(const SolveDims &d, const DevCsr &J, const StepP &P, int offset,
-                    cudaStream_t s)
+int g_nsm = 0;
+
+template <class K>
+cudaError_t launch_grid(K kern, const SolveDims &d, int64_t items, size_t smem, cudaStream_t s,
+                        const StepP &P, int offset)
 {
-    const dim3 grid((unsigned)((d.n * d.W + 7) / 8)), block(256);
-    if (KIND == K_XY) return launch(k_step<T, KIND, WIN, W_UNIT>, grid, block, s, d.pdl, P, offset);
-    if (J.unit) return launch(k_step<T, KIND, WIN, W_UNIT>, grid, block, s, d.pdl, P, offset);
-    if (d.prec == P_F64) return launch(k_step<T, KIND, WIN, W_F64>, grid, block, s, d.pdl, P, offset);
-    return launch(k_step<T, KIND, WIN, W_F32>, grid, block, s, d.pdl, P, offset);
+    if (!g_nsm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_nsm, cudaDevAttrMultiProcessorCount, dev);
+    }
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem);
+    if (per_sm < 1) per_sm = 1;
+    int64_t blocks = (items + 7) / 8;
+    if (blocks > (int64_t)g_nsm * per_sm) blocks = (int64_t)g_nsm * per_sm;
+    return launch(kern, dim3((unsigned)blocks), dim3(256), smem, s, d.pdl, P, offset);
+}
+
+template <class T, int V, int KIND, bool WIN>
+cudaError_t step_v(const SolveDims &d, const DevCsr &J, const StepP &P, int offset, cudaStream_t s)
+{
+    const int64_t items = d.n * (d.Ap / (32 * V));
+    const size_t smem = WIN ? sizeof(uint32_t) * d.W : 0;
+    const bool big = J.max_deg > 224;
+    if (KIND == K_XY || J.unit) {
+        if (big) return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, true>, d, items, smem, s, P, offset);
+        return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, false>, d, items, smem, s, P, offset);
+    }
+    if constexpr (sizeof(T) == 8)
+        return launch_grid(k_row<T, V, KIND, WIN, W_F64, false>, d, items, smem, s, P, offset);
+    else
+        return launch_grid(k_row<T, V, KIND, WIN, W_F32, false>, d, items, smem, s, P, offset);
+}
+
+// Agents per lane: a 16-byte vector when the padded agent count allows.
+template <class T> int pick_v(int Ap)
+{
+    int v = 16 / (int)sizeof(T);
+    while (v > 1 && Ap % (32 * v)) v >>= 1;
+    return v;
+}
+
+template <class T, int KIND, bool WIN>
+cudaError_t step_kw(const SolveDims &d, const DevCsr &J, const StepP &P, int offset, cudaStream_t s)
+{
+    switch (pick_v<T>(d.Ap)) {
+    case 8:
+        if constexpr (sizeof(T) == 2) return step_v<T, 8, KIND, WIN>(d, J, P, offset, s);
+        else return cudaErrorInvalidValue;
+    case 4:
+        if constexpr (sizeof(T) <= 4) return step_v<T, 4, KIND, WIN>(d, J, P, offset, s);
+        else return cudaErrorInvalidValue;
+    case 2: return step_v<T, 2, KIND, WIN>(d, J, P, offset, s);
+    default: return step_v<T, 1, KIND, WIN>(d, J, P, offset, s);
+    }
 }
 
 template <class T>
 cudaError_t step_t(const SolveDims &d, const DevCsr &J, const StepP &P, int kind, bool win,
                    int offset, cudaStream_t s)
 {
-    if (kind == K_XY) return step_wm<T, K_XY, false>(d, J, P, offset, s);
+    if (kind == K_XY) return step_kw<T, K_XY, false>(d, J, P, offset, s);
     if (kind == K_FUSED)
-        return win ? step_wm<T, K_FUSED, true>(d, J, P, offset, s)
-                   : step_wm<T, K_FUSED, false>(d, J, P, offset, s);
-    return win ? step_wm<T, K_FC, true>(d, J, P, offset, s)
-               : step_wm<T, K_FC, false>(d, J, P, offset, s);
+        return win ? step_kw<T, K_FUSED, true>(d, J, P, offset, s)
+                   : step_kw<T, K_FUSED, false>(d, J, P, offset, s);
+    return win ? step_kw<T, K_FC, true>(d, J, P, offset, s) : step_kw<T, K_FC, false>(d, J, P, offset, s);
 }
 
 cudaError_t step(const SolveDims &d, const DevCsr &J, const StepP &P, int kind, bool win,
@@ -341,9 +472,9 @@ cudaError_t launch_chunk(const SolveDims &d, const DevCsr &J, Work &w, cudaStrea
     Q.threshold = d.threshold;
     Q.period = d.period;
     Q.uw = d.uw;
-    e = launch(k_win_agents, dim3((unsigned)((d.W * 32 + 255) / 256)), dim3(256), s, d.pdl, Q);
+    e = launch(k_win_agents, dim3((unsigned)((d.W * 32 + 255) / 256)), dim3(256), 0, s, d.pdl, Q);
     if (e != cudaSuccess) return e;
-    e = launch(k_win_snap, dim3((unsigned)((d.n * d.W + 255) / 256)), dim3(256), s, d.pdl, Q);
+    e = launch(k_win_snap, dim3((unsigned)((d.n * d.W + 255) / 256)), dim3(256), 0, s, d.pdl, Q);
     *launches += 2;
     return e;
 }

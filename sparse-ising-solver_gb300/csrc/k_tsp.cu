@@ -33,7 +33,7 @@ struct TspP {
     int32_t *stab;
     uint8_t *bif, *prev;
     int32_t *ctl;
-    int32_t N, A, Ap, W, steps, period, threshold;
+    int32_t N, A, Ap, W, nwin, period, threshold;
     float qa8, qb4, qc4;              // A/8, B/4, C/4
     float dtxi0, dt, k1u, k2u;        // pre-step Update_XY coefficients
 };
@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(512) k_tsp_resident(const TspP P, const int KA
     (void)bits0;
     __syncthreads();
 
-    const int nwin = P.period > 0 ? (P.steps + P.period - 1) / P.period : 1;
+    const int nwin = P.nwin;
     const uint32_t maskN = N == 32 ? 0xffffffffu : ((1u << N) - 1u);
     int k_step = 0;
     for (int wdx = 0; wdx < nwin; wdx++) {
@@ -294,7 +294,7 @@ cudaError_t launch_tsp_resident(const SolveDims &d, const DevTsp &t, Work &w, in
     P.A = d.A;
     P.Ap = d.Ap;
     P.W = d.W;
-    P.steps = d.steps;
+    P.nwin = d.nwin;
     P.period = d.period;
     P.threshold = d.threshold;
     P.qa8 = (float)(t.A / 8);
@@ -479,7 +479,7 @@ cudaError_t stream_t(const SolveDims &d, const DevTsp &t, Work &w, const double2
     Q.W = d.W;
     Q.threshold = d.threshold;
     void *cur = w.x, *nxt = w.x2;
-    const int nwin = d.period > 0 ? (d.steps + d.period - 1) / d.period : 1;
+    const int nwin = d.nwin;
     int k = 0;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)((n * d.W + 7) / 8));

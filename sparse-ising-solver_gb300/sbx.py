@@ -36,7 +36,7 @@ class Params(C.Structure):
                 ("fused", C.c_int32), ("update_window", C.c_int32), ("period", C.c_int32),
                 ("threshold", C.c_int32), ("precision", C.c_int32), ("seed", C.c_uint32),
                 ("kernel", C.c_int32), ("agents_per_block", C.c_int32), ("trace", C.c_int32),
-                ("flags", C.c_uint32)]
+                ("flags", C.c_uint32), ("run_steps", C.c_int32)]
 
 
 class Result(C.Structure):
