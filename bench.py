@@ -153,7 +153,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--sb-steps", type=int, default=CONFIG["sb_steps"],
+                    help="SB steps per solve (profiling cases use fewer)")
+    ap.add_argument("--legs", default="all", choices=["all", "bf16"],
+                    help="bf16: only the timed BF16 solves (profiling)")
     args = ap.parse_args()
+    CONFIG["sb_steps"] = args.sb_steps
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -222,6 +227,12 @@ def main():
         return units / (ms / 1000.0), ms / k, res, vals, clk.summary(), launches // max(k, 1)
 
     v_bf16, ms_bf16, r_bf16, cuts_bf16, clocks, launches = timed(sbx.BF16, args.steps, args.warmup)
+    if args.legs == "bf16":
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": v_bf16, "ms_per_step": ms_bf16,
+                              "config": dict(CONFIG), "legs": "bf16"}), flush=True)
+        ctx.close()
+        return
     v_f32, ms_f32, r_f32, cuts_f32, _, _ = timed(sbx.F32, 1, 1)
     r64, cuts64 = ctx.solve(prob, prm(sbx.F64))
 

@@ -97,6 +97,7 @@ const char *sbx_version(void);
 void sbx_params_default(sbx_params *p);
 
 int sbx_create(sbx_ctx **ctx, int device);
+/* Problems outlive their context only as handles to destroy. */
 int sbx_destroy(sbx_ctx *ctx);
 /* Run on a caller's cudaStream_t (passed as void*); NULL selects the
  * context's own stream. */

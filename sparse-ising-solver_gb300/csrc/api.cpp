@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstring>
 #include <numeric>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -46,6 +47,7 @@ struct sbx_ctx {
     SolveDims d;
     int32_t N = 0;
     std::string err;
+    std::set<sbx_problem *> problems;   // live problems; orphaned on destroy
 };
 
 namespace {
@@ -689,6 +691,7 @@ int sbx_destroy(sbx_ctx *ctx)
     for (auto &e : ctx->prof) cudaEventDestroy(e);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->own) cudaStreamDestroy(ctx->own);
+    for (sbx_problem *p : ctx->problems) p->ctx = nullptr;   // they stay valid to destroy
     delete ctx;
     return SBX_OK;
 }
@@ -716,6 +719,7 @@ int sbx_problem_csr(sbx_ctx *ctx, int64_t n, int64_t nnz, const int32_t *rowptr,
         delete p;
         return rc;
     }
+    ctx->problems.insert(p);
     *out = p;
     return SBX_OK;
 }
@@ -806,6 +810,7 @@ int sbx_problem_tsp(sbx_ctx *ctx, int32_t N, const double *packed, double A, dou
         delete p;
         return rc;
     }
+    ctx->problems.insert(p);
     *out = p;
     return SBX_OK;
 }
@@ -813,10 +818,13 @@ int sbx_problem_tsp(sbx_ctx *ctx, int32_t N, const double *packed, double A, dou
 int sbx_problem_destroy(sbx_problem *p)
 {
     if (!p) return SBX_ERR_ARG;
-    if (p->ctx && p->ctx->gexec) {   // a cached graph may point at this problem
-        cudaGraphExecDestroy(p->ctx->gexec);
-        p->ctx->gexec = nullptr;
-        p->ctx->gkey.clear();
+    if (p->ctx) {
+        p->ctx->problems.erase(p);
+        if (p->ctx->gexec) {   // a cached graph may point at this problem
+            cudaGraphExecDestroy(p->ctx->gexec);
+            p->ctx->gexec = nullptr;
+            p->ctx->gkey.clear();
+        }
     }
     free_csr(p->J);
     free_csr(p->T.qubo);
@@ -841,6 +849,7 @@ int sbx_solve(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
               double *agent_values)
 {
     if (!ctx || !p || !pr || !res) return fail(ctx, SBX_ERR_ARG, "null argument");
+    if (p->ctx != ctx) return fail(ctx, SBX_ERR_ARG, "problem belongs to another (or a destroyed) context");
     if (pr->agents < 1 || pr->steps < 0 || !(pr->dt == pr->dt) || pr->precision < 0 ||
         pr->precision > 3 || pr->run_steps < 0 || pr->period < 0 || pr->threshold < 0)
         return fail(ctx, SBX_ERR_ARG, "bad params (agents >= 1, steps >= 0, precision 0..3)");

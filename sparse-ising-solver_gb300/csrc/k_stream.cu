@@ -91,6 +91,11 @@ template <class T, int V> __device__ __forceinline__ void vstore(T *p, const T (
 // hold 7 chunks of 32 neighbours; BIG rows (degree > 224) flush them into ints.
 // The new signs of the V agents are OR-combined across the lanes of a word
 // and written once.
+// x + a*b: one FMA in FP32; in FP64 two separately rounded operations, the
+// reference's arithmetic as the oracle states it.
+__device__ __forceinline__ float madd(float a, float b, float x) { return fmaf(a, b, x); }
+__device__ __forceinline__ double madd(double a, double b, double x) { return __dadd_rn(x, __dmul_rn(a, b)); }
+
 template <class T, int V, int KIND, bool WIN, int WM, bool BIG>
 __global__ void __launch_bounds__(256) k_row(const StepP P, const int offset)
 {
@@ -111,13 +116,21 @@ __global__ void __launch_bounds__(256) k_row(const StepP P, const int offset)
     uint32_t *Snext = (step & 1) ? P.S0 : P.S1;
     constexpr int G = 32 / V;   // lanes sharing one sign word
     constexpr uint32_t VM = (V == 32) ? 0xffffffffu : ((1u << V) - 1u);
+    // Items (row, segment) in steps of the warp count, advanced without
+    // divisions: r += nw / nit, it += nw % nit with carry.
     const int nit = P.Ap / (32 * V);
-    const int64_t items = P.n * nit;
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t item = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); item < items;
-         item += nw) {
-        const int64_t r = item / nit;
-        const int it = (int)(item - r * nit);
+    const int64_t w0 = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int64_t dr = nw / nit;
+    const int dit = (int)(nw - dr * nit);
+    int64_t r = w0 / nit;
+    int it = (int)(w0 - r * nit);
+    for (; r < P.n; r += dr, it += dit) {
+        if (it >= nit) {
+            it -= nit;
+            r++;
+            if (r >= P.n) break;
+        }
         const int a0 = it * 32 * V + lane * V;
         const int q = a0 >> 5, off = a0 & 31;
         const int64_t base = r * P.Ap + a0;
@@ -134,8 +147,8 @@ __global__ void __launch_bounds__(256) k_row(const StepP P, const int offset)
             for (int v = 0; v < V; v++) {
                 x[v] = St<T>::ld(xs[v]);
                 y[v] = St<T>::ld(ys[v]);
-                y[v] = add(y[v], mul((A)c.w, x[v]));
-                x[v] = add(x[v], mul((A)c.z, y[v]));
+                y[v] = madd((A)c.w, x[v], y[v]);
+                x[v] = madd((A)c.z, y[v], x[v]);
             }
         } else {
             const int32_t e0 = __ldg(&P.rowptr[r]), e1 = __ldg(&P.rowptr[r + 1]);
@@ -154,16 +167,20 @@ __global__ void __launch_bounds__(256) k_row(const StepP P, const int offset)
                 R myv = R(0);
                 if (WM == W_F32) myv = lane < m ? __ldg(&P.valf[cb + lane]) : 0.f;
                 if (WM == W_F64) myv = lane < m ? __ldg(&P.vald[cb + lane]) : 0.0;
+                const uint32_t *Sq = Scur + q;
 #pragma unroll 4
                 for (int k = 0; k < m; k++) {
                     const uint32_t cw = __shfl_sync(FULL, mycw, k);
-                    const uint32_t word = __ldg(&Scur[(int64_t)(cw & 0x7fffffffu) * P.W + q]);
-                    uint32_t bits = (word >> off) & VM;
+                    const uint32_t word = __ldg(Sq + (size_t)(cw & 0x7fffffffu) * (size_t)P.W);
+                    uint32_t bits = word >> off;
                     if (WM == W_UNIT) {
-                        bits ^= (0u - (cw >> 31)) & VM;
+                        // weight sign -> all-ones mask; unused high bits only
+                        // reach counter bytes that are never read
+                        bits ^= (uint32_t)((int32_t)cw >> 31);
                         lo += spread4(bits & 0xfu);
-                        if (V == 8) hi += spread4(bits >> 4);
+                        if (V == 8) hi += spread4((bits >> 4) & 0xfu);
                     } else {
+                        bits &= VM;
                         const R wv = __shfl_sync(FULL, myv, k);
 #pragma unroll
                         for (int v = 0; v < V; v++) {
@@ -200,22 +217,22 @@ __global__ void __launch_bounds__(256) k_row(const StepP P, const int offset)
                         x[v] = spin_of(x[v]);
                         y[v] = A(0);
                     } else {
-                        y[v] = add(y[v], mul(c0, total));
+                        y[v] = madd(c0, total, y[v]);
                     }
-                    x[v] = add(x[v], mul((A)c.x, y[v]));
-                    y[v] = add(y[v], mul((A)c.y, x[v]));
+                    x[v] = madd((A)c.x, y[v], x[v]);
+                    y[v] = madd((A)c.y, x[v], y[v]);
                 } else {
                     // mat_mult (:207) and confine (:158-165) of this step, then
                     // Update_XY of the next one unless the window closes here.
-                    y[v] = add(y[v], mul(c0, total));
+                    y[v] = madd(c0, total, y[v]);
                     if (fabs(x[v]) > A(1)) {
                         x[v] = spin_of(x[v]);
                         y[v] = A(0);
                     }
                     if (!WIN) {
                         const auto cn = Coef<A>::get(P, step + 1);
-                        y[v] = add(y[v], mul((A)cn.w, x[v]));
-                        x[v] = add(x[v], mul((A)cn.z, y[v]));
+                        y[v] = madd((A)cn.w, x[v], y[v]);
+                        x[v] = madd((A)cn.z, y[v], x[v]);
                     }
                 }
             }
