@@ -138,6 +138,28 @@ int sbx_solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems,
                     const int32_t *agents, const sbx_params *params,
                     sbx_result *res, double *agent_values, double *batch_time_us);
 
+/* ---- fused steps without device allocation ---- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory (a process whose device memory is all held by its own arena, or a
+ * loop that cannot take cudaMalloc's synchronisation): runs fused SB steps
+ * step0 .. step0+nsteps-1 of a max_steps schedule (FP32 state, any float
+ * weights, src/kernels.cu:211-269 in Jacobi order) on caller-owned device
+ * buffers -- CSR d_rowptr[n+1], d_col[nnz], d_val[nnz]; d_x, d_y [n][agents],
+ * updated in place -- on cuda_stream (NULL: the legacy default stream).  Its
+ * only scratch, two sign planes, lives in a static device array of
+ * 2 * SBX_NOALLOC_MAX_WORDS words (16 MiB, held by every GPU that loads the
+ * library); n * agents / 32 must not exceed SBX_NOALLOC_MAX_WORDS and agents
+ * must be a multiple of 32, else SBX_ERR_ARG.  The first call on a device
+ * looks up the array's device address (make it before any stream capture);
+ * calls share the array, so calls that overlap on the GPU race.  Nothing is
+ * allocated or freed. */
+#define SBX_NOALLOC_MAX_WORDS (1 << 21)
+int sbx_fused_steps_noalloc(const int32_t *d_rowptr, const int32_t *d_col,
+                            const float *d_val, int64_t n, int32_t agents,
+                            float *d_x, float *d_y, double dt, double xi0,
+                            int32_t step0, int32_t nsteps, int32_t max_steps,
+                            void *cuda_stream);
+
 /* ---- host-side loaders (no device needed) ---- */
 /* csr.cpp:15-109: two-call protocol, first with NULL arrays for the sizes. */
 int sbx_load_mtx(const char *path, int64_t *n, int64_t *nnz, int32_t *rowptr,

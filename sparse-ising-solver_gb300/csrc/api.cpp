@@ -615,6 +615,11 @@ float f16_to_f(uint16_t h)
 
 }  // namespace
 
+namespace sbx {
+// Lets the other translation units of the library report through sbx_last_error.
+void set_last_error(const std::string &m) { g_err = m; }
+}  // namespace sbx
+
 extern "C" {
 
 const char *sbx_strerror(int status)

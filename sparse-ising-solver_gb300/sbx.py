@@ -19,6 +19,7 @@ KERNEL_AUTO, KERNEL_STREAM, KERNEL_RESIDENT = 0, 1, 2
 DIST_EUC_2D, DIST_GEO, DIST_EUC_2D_FLOAT = 0, 1, 2
 FLAG_NO_PDL, FLAG_NO_GRAPH, FLAG_PROFILE = 1, 2, 4
 PRECISIONS = {"f32": F32, "bf16": BF16, "f16": F16, "f64": F64}
+NOALLOC_MAX_WORDS = 1 << 21   # SBX_NOALLOC_MAX_WORDS in include/sbx.h
 
 # Every function include/sbx.h declares (checked by the CPU tests).
 EXPORTS = [
@@ -27,7 +28,7 @@ EXPORTS = [
     "sbx_problem_destroy", "sbx_problem_info", "sbx_solve", "sbx_get_state", "sbx_get_tours",
     "sbx_get_trace", "sbx_solve_batch", "sbx_load_mtx", "sbx_load_tsplib",
     "sbx_tsp_distances", "sbx_gen_er", "sbx_gen_torus", "sbx_gen_rmat", "sbx_gen_rgg",
-    "sbx_gen_cities",
+    "sbx_gen_cities", "sbx_fused_steps_noalloc",
 ]
 
 
