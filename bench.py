@@ -1,17 +1,19 @@
 """Benchmark of the SB hot path: nnz*agent*steps/s on one GB300.
 
-Workload (the metric's headline configuration): MaxCut on a 2-D torus 100x100
-(n = 10,000, degree 4, weights +-1 from seed 1234), 1024 agents, dt = 0.5,
-fused kernel, 20,000 steps, update window on (early exit once every agent has
-bifurcated).  A bench "step" is one complete solve of that instance (device
-init from the seed, the SB loop, windows, the cut reduction).  `value` is the
-BF16-state run with the problem resident on the device; the FP32-state run of
-the same instance and the FP64 run (energy-error reference) are reported
-beside it.  `e2e` repeats the BF16 solve through the C ABI from host buffers:
-the CSR upload, the solve and the per-agent cut read-back are inside the timed
-region.
+Default workload (the metric's headline configuration): MaxCut on a 2-D torus
+100x100 (n = 10,000, degree 4, weights +-1 from seed 1234), 1024 agents,
+dt = 0.5, fused kernel, 20,000 steps, update window on (early exit once every
+agent has bifurcated).  A bench "step" is one complete solve of the instance
+(device init from the seed, the SB loop, windows, the cut reduction).
+`value` is the BF16-state run with the problem resident on the device; the
+FP32 run and the FP64 run (the energy-error reference) of the same seed are
+reported beside it.  `e2e` repeats the BF16 solve through the C ABI from host
+buffers: CSR upload, solve and per-agent cut read-back are inside the timed
+region.  Other workloads (--workload): er800 (ER n=800, FP32 plain, 10k
+steps), rmat20 (R-MAT 2^20, 256 agents, BF16), tsp30 (30 cities, FP32).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload torus|er800|rmat20|tsp30]
 """
 import argparse
 import json
@@ -28,9 +30,22 @@ for p in (PKG, ORACLE):
     if p not in sys.path:
         sys.path.insert(0, p)
 
-CONFIG = dict(workload="maxcut-torus-100x100-pm1", n=10000, degree=4, agents=1024, dt=0.5,
-              sb_steps=20000, update_window=1, fused=1, graph_seed=1234, init_seed=1)
 METRIC = "nnz*agent*steps/s"
+WORKLOADS = {
+    "torus": dict(kind="maxcut", workload="maxcut-torus-100x100-pm1", graph=("torus", 100, 100),
+                  agents=1024, dt=0.5, sb_steps=20000, update_window=1, fused=1,
+                  precision="bf16", compare=("f32", "f64")),
+    "er800": dict(kind="maxcut", workload="maxcut-er-800-p0.0601-unit",
+                  graph=("er", 800, 0.0601, False), agents=1024, dt=0.1, sb_steps=10000,
+                  update_window=0, fused=1, precision="f32", compare=("bf16", "f64")),
+    "rmat20": dict(kind="maxcut", workload="maxcut-rmat-scale20-ef4-unit",
+                   graph=("rmat", 20, 4), agents=256, dt=0.5, sb_steps=10000, update_window=0,
+                   fused=1, precision="bf16", compare=("f32",)),
+    "tsp30": dict(kind="tsp", workload="tsp-30-unit-square-penalty1.5maxd", cities=30,
+                  agents=1024, dt=0.1, sb_steps=20000, precision="f32", compare=("bf16",)),
+}
+GRAPH_SEED, INIT_SEED = 1234, 1
+PBYTES = {"f32": 4, "bf16": 2, "f16": 2, "f64": 8}
 
 
 def load_peaks():
@@ -51,6 +66,7 @@ class Clocks:
     def __init__(self, device):
         self.device = device
         self.proc = None
+        self.lines = []
 
     def __enter__(self):
         try:
@@ -63,7 +79,6 @@ class Clocks:
         return self
 
     def __exit__(self, *a):
-        self.lines = []
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -76,7 +91,7 @@ class Clocks:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for l in getattr(self, "lines", []):
+        for l in self.lines:
             f = [x.strip() for x in l.split(",")]
             if len(f) < 9:
                 continue
@@ -92,41 +107,88 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sample(g, A, sb_steps, seconds=12.0, nthreads=0):
-    """The FP64 oracle (OpenMP over rows, all host threads) on a bounded sample
-    of the workload: the same graph and agents for `s` SB steps."""
+def build_instance(wl):
+    """The seeded synthetic instance: a Graph, or a dict with the TSP data."""
+    import sbx
+    if wl["kind"] == "maxcut":
+        g = wl["graph"]
+        if g[0] == "torus":
+            return sbx.gen_torus(g[1], g[2], seed=GRAPH_SEED)
+        if g[0] == "er":
+            return sbx.gen_er(g[1], g[2], pm1=g[3], seed=GRAPH_SEED)
+        return sbx.gen_rmat(g[1], g[2], seed=GRAPH_SEED)
+    xc, yc = sbx.gen_cities(wl["cities"], 1.0, seed=GRAPH_SEED)
+    packed = sbx.tsp_distances(xc, yc, sbx.DIST_EUC_2D_FLOAT)
+    mx = float(packed.max())
+    return dict(xc=xc, yc=yc, packed=packed, N=wl["cities"], A=1.0, B=1.5 * mx, C=1.5 * mx)
+
+
+def oracle_tsp(inst):
     import sbo
-    og = sbo.Graph(g.n, g.rowptr, g.col, g.val, g.wsum)
-    t = []
-    for k in (2, 6):   # the difference removes the init cost
-        t0 = time.perf_counter()
-        sbo.maxcut_solve(og, sbo.params(dt=CONFIG["dt"], steps=k, period=k, agents=A,
-                                        seed=CONFIG["init_seed"], nthreads=nthreads))
-        t.append(time.perf_counter() - t0)
-    per_step = max((t[1] - t[0]) / 4.0, 1e-4)
-    s = int(max(2, min(sb_steps, seconds / per_step)))
-    t0 = time.perf_counter()
-    o = sbo.maxcut_solve(og, sbo.params(dt=CONFIG["dt"], steps=s, period=s, agents=A,
-                                        seed=CONFIG["init_seed"], nthreads=nthreads))
-    dt = time.perf_counter() - t0
-    cores = nthreads if nthreads > 0 else (os.cpu_count() or 1)
-    return g.nnz * A * o["result"]["steps_run"] / dt, cores, s, dt
+    return sbo.Tsp(inst["xc"], inst["yc"], sbo.DIST_EUC_2D_FLOAT, A=inst["A"], B=inst["B"],
+                   C_=inst["C"])
 
 
-def run_reference(args, rank):
+def instance_sizes(wl, inst):
+    if wl["kind"] == "maxcut":
+        return inst.n, inst.nnz
+    t = oracle_tsp(inst)
+    return t.graph.n, t.graph.nnz
+
+
+def config_of(wl):
+    c = {k: v for k, v in wl.items() if k not in ("compare", "graph")}
+    if "graph" in wl:
+        c["graph"] = list(wl["graph"])
+    c["graph_seed"], c["init_seed"] = GRAPH_SEED, INIT_SEED
+    return c
+
+
+def cpu_sample(wl, inst, seconds=12.0, nthreads=0):
+    """The FP64 oracle on a bounded sample of the workload: the same instance
+    and agents for s SB steps (OpenMP over rows, every host thread, for MaxCut;
+    one thread for TSP).  Returns (nnz*agent*steps/s, cores, s, seconds)."""
+    import sbo
+    A = wl["agents"]
+    if wl["kind"] == "maxcut":
+        og = sbo.Graph(inst.n, inst.rowptr, inst.col, inst.val, inst.wsum)
+        nnz = inst.nnz
+        cores = nthreads if nthreads > 0 else (os.cpu_count() or 1)
+
+        def run(k):
+            t0 = time.perf_counter()
+            o = sbo.maxcut_solve(og, sbo.params(dt=wl["dt"], steps=k, period=k, agents=A,
+                                                seed=INIT_SEED, nthreads=nthreads))
+            return time.perf_counter() - t0, o["result"]["steps_run"]
+    else:
+        t = oracle_tsp(inst)
+        nnz = t.graph.nnz
+        cores = 1
+
+        def run(k):
+            t0 = time.perf_counter()
+            o = t.solve(sbo.params(dt=wl["dt"], steps=k, agents=A, seed=INIT_SEED, threshold=50))
+            return time.perf_counter() - t0, o["result"]["steps_run"]
+    ta, _ = run(10)
+    tb, _ = run(30)   # the difference removes the init cost
+    per_step = max((tb - ta) / 20.0, 1e-5)
+    s = int(max(10, min(wl["sb_steps"], seconds / per_step)))
+    s = (s // 10) * 10
+    dt, steps = run(s)
+    return nnz * A * steps / dt, cores, s, dt
+
+
+def run_reference(args, wl, rank):
     """--impl reference: the reference path has no CPU solver, so its CPU
-    implementation here is the FP64 oracle port, all host threads."""
+    implementation here is the FP64 oracle port, every host thread."""
     if rank != 0:
         return
-    import sbx
     import sbo
     sbo.lib()
-    g = sbx.gen_torus(100, 100, seed=CONFIG["graph_seed"])
-    A = CONFIG["agents"]
-    vals = []
-    samples = []
+    inst = build_instance(wl)
+    vals, samples, cores = [], [], 1
     for i in range(args.warmup + args.steps):
-        v, cores, s, dt = cpu_sample(g, A, CONFIG["sb_steps"], seconds=8.0)
+        v, cores, s, dt = cpu_sample(wl, inst, seconds=8.0)
         if i >= args.warmup:
             vals.append(v)
             samples.append((s, dt))
@@ -136,7 +198,7 @@ def run_reference(args, rank):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * sum(d for _, d in samples) / len(samples),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": dict(CONFIG),
+        "data": "synthetic (seeded generators)", "config": config_of(wl),
         "cpu_baseline": {"value": value, "unit": "nnz*agent*steps/s", "cores": cores,
                          "kind": "port",
                          "sample": "%d SB steps of the workload per bench step" % samples[0][0]},
@@ -152,22 +214,24 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="torus", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
-    ap.add_argument("--sb-steps", type=int, default=CONFIG["sb_steps"],
+    ap.add_argument("--sb-steps", type=int, default=0,
                     help="SB steps per solve (profiling cases use fewer)")
-    ap.add_argument("--legs", default="all", choices=["all", "bf16"],
-                    help="bf16: only the timed BF16 solves (profiling)")
+    ap.add_argument("--legs", default="all", choices=["all", "main"],
+                    help="main: only the timed solves of the main precision (profiling)")
     args = ap.parse_args()
-    CONFIG["sb_steps"] = args.sb_steps
+    wl = dict(WORKLOADS[args.workload])
+    if args.sb_steps:
+        wl["sb_steps"] = args.sb_steps
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
-        run_reference(args, rank)
+        run_reference(args, wl, rank)
         return
 
-    import numpy as np
     import torch
     import sbx
 
@@ -182,25 +246,34 @@ def main():
     torch.cuda.set_stream(stream)
     ctx = sbx.Context(local)
     ctx.set_stream(stream.cuda_stream)
-    g = sbx.gen_torus(100, 100, seed=CONFIG["graph_seed"])
-    A = CONFIG["agents"]
-    prob = ctx.problem(g)
-    seed = CONFIG["init_seed"] + rank   # each rank: an independent replica (weak scaling)
+    inst = build_instance(wl)
+    A = wl["agents"]
+    n, nnz = instance_sizes(wl, inst)
+
+    def make_problem():
+        if wl["kind"] == "maxcut":
+            return ctx.problem(inst)
+        return ctx.tsp_problem(inst["packed"], inst["N"], A=inst["A"], B=inst["B"], C_=inst["C"])
+
+    prob = make_problem()
+    seed = INIT_SEED + rank   # each rank: an independent replica (weak scaling)
 
     def prm(prec, flags=0):
-        return sbx.params(dt=CONFIG["dt"], steps=CONFIG["sb_steps"], agents=A,
-                          fused=CONFIG["fused"], update_window=CONFIG["update_window"],
-                          seed=seed, precision=prec, flags=flags)
+        kw = dict(dt=wl["dt"], steps=wl["sb_steps"], agents=A, seed=seed,
+                  precision=sbx.PRECISIONS[prec], flags=flags)
+        if wl["kind"] == "maxcut":
+            kw.update(fused=wl["fused"], update_window=wl["update_window"])
+        return sbx.params(**kw)
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def quality(r):
+        return r["max"] if wl["kind"] == "maxcut" else r["min"]
 
     def timed(prec, k, w):
         for _ in range(w):
             ctx.solve(prob, prm(prec))
-        evs = []
-        units = 0
-        launches = 0
-        res = None
+        evs, units, launches, res = [], 0, 0, None
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
@@ -210,10 +283,10 @@ def main():
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-                res, vals = ctx.solve(prob, prm(prec))
+                res, _ = ctx.solve(prob, prm(prec))
                 e1.record(stream)
                 evs.append((e0, e1))
-                units += g.nnz * A * res["steps_run"]
+                units += nnz * A * res["steps_run"]
                 launches += res["gpu_launches"]
             torch.cuda.synchronize()
         ms = sum(a.elapsed_time(b) for a, b in evs)
@@ -224,77 +297,101 @@ def main():
             u = torch.tensor([units], device="cuda", dtype=torch.float64)
             dist.all_reduce(u)
             units = float(u.item())
-        return units / (ms / 1000.0), ms / k, res, vals, clk.summary(), launches // max(k, 1)
+        return units / (ms / 1000.0), ms / k, res, clk.summary(), launches // max(k, 1)
 
-    v_bf16, ms_bf16, r_bf16, cuts_bf16, clocks, launches = timed(sbx.BF16, args.steps, args.warmup)
-    if args.legs == "bf16":
+    main_prec = wl["precision"]
+    v_main, ms_main, r_main, clocks, launches = timed(main_prec, args.steps, args.warmup)
+    if args.legs == "main":
         if rank == 0:
-            print(json.dumps({"metric": METRIC, "value": v_bf16, "ms_per_step": ms_bf16,
-                              "config": dict(CONFIG), "legs": "bf16"}), flush=True)
+            print(json.dumps({"metric": METRIC, "value": v_main, "ms_per_step": ms_main,
+                              "config": config_of(wl), "legs": "main"}), flush=True)
         ctx.close()
         return
-    v_f32, ms_f32, r_f32, cuts_f32, _, _ = timed(sbx.F32, 1, 1)
-    r64, cuts64 = ctx.solve(prob, prm(sbx.F64))
 
-    # e2e: through the C ABI from host buffers, CSR upload + solve + read-back.
-    t_e2e = []
-    units_e2e = 0
+    # The same solve in the other precisions: throughput and best result.
+    others = {}
+    for prec in wl["compare"]:
+        if prec == "f64":
+            rr, _ = ctx.solve(prob, prm("f64"))
+            others["f64"] = {"best": quality(rr), "steps_run": rr["steps_run"],
+                             "ms": rr["time_us"] / 1000.0}
+        else:
+            v, ms, rr, _, _ = timed(prec, 1, 1)
+            others[prec] = {"value": v, "ms_per_step": ms, "best": quality(rr),
+                            "steps_run": rr["steps_run"]}
+
+    # e2e: through the C ABI from host buffers, upload + solve + read-back.
+    t_e2e, units_e2e = [], 0
     for i in range(args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        p2 = ctx.problem(g)
-        r2, _ = ctx.solve(p2, prm(sbx.BF16))
+        p2 = make_problem()
+        r2, _ = ctx.solve(p2, prm(main_prec))
         p2.close()
         torch.cuda.synchronize()
         if i >= args.warmup:
             t_e2e.append(time.perf_counter() - t0)
-            units_e2e += g.nnz * A * r2["steps_run"]
+            units_e2e += nnz * A * r2["steps_run"]
     e2e = units_e2e / sum(t_e2e)
+    if wl["kind"] == "maxcut":
+        h2d = int(inst.rowptr.nbytes + inst.col.nbytes + inst.val.nbytes)
+    else:
+        h2d = int(inst["packed"].nbytes)
+    d2h = int(8 * A + 64)
 
-    # Dominant kernel: the streaming step kernel, timed launch by launch.
-    rp, _ = ctx.solve(prob, prm(sbx.BF16, sbx.FLAG_PROFILE))
+    # Dominant kernel, timed launch by launch (SBX_FLAG_PROFILE).
+    rp, _ = ctx.solve(prob, prm(main_prec, sbx.FLAG_PROFILE))
     peaks, peak_kind = load_peaks()
-    sx = sy = 2
-    b_step = 2 * g.n * A * (sx + sy) + 8 * g.nnz + 4 * (g.n + 1)
+    s = PBYTES[main_prec]
+    b_step = 2 * n * A * (s + s) + 8 * nnz + 4 * (n + 1)
     roof = None
     if rp["kernel_launches"] and rp["kernel_ms"] > 0:
         per_launch_s = rp["kernel_ms"] / 1000.0 / rp["kernel_launches"]
-        achieved = b_step / per_launch_s / 1e9
+        if rp["kernel_used"] == sbx.KERNEL_STREAM:
+            bytes_per_launch, kname = b_step, "k_row (one SB step per launch)"
+        else:
+            bytes_per_launch = b_step * rp["steps_run"]
+            kname = "resident (whole solve per launch; state on chip, effective bytes)"
+        achieved = bytes_per_launch / per_launch_s / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": None,
-                "peak_kind": peak_kind, "kernel": "k_step<bf16,fused>",
-                "bytes_per_launch": b_step, "launch_us": per_launch_s * 1e6}
+                "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_kind": peak_kind,
+                "kernel": kname, "bytes_per_launch": bytes_per_launch,
+                "launch_us": per_launch_s * 1e6, "launches": rp["kernel_launches"]}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        v, cores, s, dt = cpu_sample(g, A, CONFIG["sb_steps"])
+        v, cores, s_cpu, dt = cpu_sample(wl, inst)
         cpu = {"value": v, "unit": "nnz*agent*steps/s", "cores": cores, "kind": "port",
-               "sample": "FP64 oracle, %d SB steps of the workload (%.1f s)" % (s, dt)}
+               "sample": "FP64 oracle, %d SB steps of the workload (%.1f s)" % (s_cpu, dt)}
 
     if rank == 0:
-        best64 = r64["max"]
+        refk = "f64" if "f64" in others else ("f32" if "f32" in others else None)
+        ref = others.get(refk) if refk else None
+        err = None
+        if ref and ref["best"] and abs(ref["best"]) < 1e300 and abs(quality(r_main)) < 1e300:
+            err = abs(quality(r_main) - ref["best"]) / abs(ref["best"])
+        qual = {"best_" + main_prec: quality(r_main), "steps_run": r_main["steps_run"],
+                "kernel": r_main["kernel_used"], "energy_error_vs_%s" % refk: err}
+        if wl["kind"] == "tsp":
+            qual["valid_agents"] = r_main["valid"]
+        else:
+            qual["ps"] = r_main["ps"]
         line = {
-            "metric": METRIC, "value": v_bf16, "unit": "nnz*agent*steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_bf16,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
-            "data": "synthetic (seeded torus, weights +-1)",
-            "config": dict(CONFIG, precision="bf16 state, fp32 arithmetic, exact integer force",
-                           l2="flushed between iterations (256 MB write)",
-                           parallelism="replicas" if world > 1 else "single"),
-            "e2e": {"value": e2e, "unit": "nnz*agent*steps/s",
-                    "h2d_bytes_per_step": int(g.rowptr.nbytes + g.col.nbytes + g.val.nbytes),
-                    "d2h_bytes_per_step": int(8 * A + 32)},
+            "metric": METRIC, "value": v_main, "unit": "nnz*agent*steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_main,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": main_prec, "data": "synthetic (seeded generators)",
+            "config": dict(config_of(wl), state="%s storage, fp32 arithmetic, exact integer force"
+                           % main_prec, l2="flushed between iterations (256 MB write)",
+                           parallelism="replicas" if world > 1 else "single", n=n, nnz=nnz),
+            "e2e": {"value": e2e, "unit": "nnz*agent*steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": clocks,
-            "fp32": {"value": v_f32, "ms_per_step": ms_f32, "best_cut": r_f32["max"],
-                     "steps_run": r_f32["steps_run"]},
-            "quality": {"best_cut_bf16": r_bf16["max"], "best_cut_fp32": r_f32["max"],
-                        "best_cut_fp64": best64,
-                        "energy_error_bf16": abs(r_bf16["max"] - best64) / abs(best64),
-                        "energy_error_fp32": abs(r_f32["max"] - best64) / abs(best64),
-                        "steps_run_bf16": r_bf16["steps_run"], "kernel": r_bf16["kernel_used"]},
+            "other_precisions": others,
+            "quality": qual,
         }
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -104,6 +104,10 @@ void free_csr(DevCsr &J)
     cudaFree(J.vald);
     cudaFree(J.valf);
     cudaFree(J.perm);
+    cudaFree(J.hchunk);
+    cudaFree(J.chunk_row);
+    J.hchunk = J.chunk_row = nullptr;
+    J.nchunks = 0;
     J.rowptr = nullptr;
     J.colw = nullptr;
     J.vald = nullptr;
@@ -171,6 +175,20 @@ int upload_csr(sbx_ctx *ctx, DevCsr &J, int64_t n, int64_t nnz, const int32_t *r
         CK(cudaMemcpy(J.valf, valf.data(), sizeof(float) * nnz, cudaMemcpyHostToDevice));
     }
     CK(cudaMemcpy(J.perm, perm.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+    if (unit && maxdeg > kHeavy) {
+        std::vector<int32_t> hchunk((size_t)n, -1), crow;
+        for (int64_t r = 0; r < n; r++) {
+            const int32_t deg = rowptr[r + 1] - rowptr[r];
+            if (deg <= kHeavy) continue;
+            hchunk[r] = (int32_t)crow.size();
+            for (int32_t c = 0; c < (deg + kHeavy - 1) / kHeavy; c++) crow.push_back((int32_t)r);
+        }
+        J.nchunks = (int32_t)crow.size();
+        CK(cudaMalloc(&J.hchunk, sizeof(int32_t) * n));
+        CK(cudaMalloc(&J.chunk_row, sizeof(int32_t) * crow.size()));
+        CK(cudaMemcpy(J.hchunk, hchunk.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(J.chunk_row, crow.data(), sizeof(int32_t) * crow.size(), cudaMemcpyHostToDevice));
+    }
     return SBX_OK;
 }
 
@@ -218,7 +236,7 @@ void stats(const std::vector<double> &v, sbx_result *r)
     r->best_agent = best;
 }
 
-int ensure_common(sbx_ctx *ctx, const SolveDims &d, int64_t total_steps)
+int ensure_common(sbx_ctx *ctx, const SolveDims &d, int64_t total_steps, int32_t J_nchunks = 0)
 {
     Work &w = ctx->w;
     const size_t es = prec_bytes(d.prec);
@@ -237,6 +255,7 @@ int ensure_common(sbx_ctx *ctx, const SolveDims &d, int64_t total_steps)
     CK(grow(w.prev, w.cap_prev, (size_t)d.Ap));
     CK(grow(w.ctl, w.cap_ctl, (size_t)CTL_N));
     CK(grow(w.eacc, w.cap_eacc, (size_t)d.Ap));
+    if (J_nchunks) CK(grow(w.part, w.cap_part, (size_t)J_nchunks * d.Ap * 2));
     CK(grow(w.cut, w.cap_cut, (size_t)d.Ap));
     const int64_t nwin = d.period > 0 ? total_steps / d.period + 2 : 2;
     CK(grow(w.wincount, w.cap_win, (size_t)nwin));
@@ -329,7 +348,7 @@ int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_r
     const int64_t nchunks = run > 0 ? (run + d.period - 1) / d.period : 0;
     const int64_t total = nchunks * d.period;
     cudaStream_t s = ctx->stream;
-    int rc = ensure_common(ctx, d, total);
+    int rc = ensure_common(ctx, d, total, p->J.nchunks);
     if (rc) return rc;
     if ((rc = upload_coef(ctx, d, total))) return rc;
     if ((rc = init_state(ctx, d, pr->seed, false))) return rc;
@@ -685,7 +704,7 @@ int sbx_destroy(sbx_ctx *ctx)
     Work &w = ctx->w;
     void *ptrs[] = {w.x, w.y, w.x2, w.S[0], w.S[1], w.Wp, w.fin, w.chg, w.newmask, w.stab, w.bif,
                     w.prev, w.ctl, w.wincount, w.visits, w.ab, w.sched, w.eacc, w.cut, w.trace,
-                    w.tours, w.valid, w.rjump, w.coef32, w.coef64};
+                    w.tours, w.valid, w.rjump, w.coef32, w.coef64, w.part};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);

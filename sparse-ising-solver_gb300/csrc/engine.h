@@ -11,6 +11,8 @@ namespace sbx {
 
 enum Prec { P_F32 = 0, P_BF16 = 1, P_F16 = 2, P_F64 = 3 };
 
+constexpr int kHeavy = 224;   // neighbours per chunk: 7 x 32, byte counters never overflow
+
 inline size_t prec_bytes(int p) { return p == P_F64 ? 8 : p == P_F32 ? 4 : 2; }
 
 // MaxCut / QUBO matrix on the device.  colw holds the column index; when every
@@ -23,6 +25,11 @@ struct DevCsr {
     double *vald = nullptr;
     float *valf = nullptr;
     int32_t *perm = nullptr; // rows in decreasing degree (resident kernel order)
+    // Heavy rows (unit weights, degree > kHeavy) are split into chunks of
+    // kHeavy neighbours whose partial counts a separate kernel computes.
+    int32_t *hchunk = nullptr;    // per row: first chunk of a heavy row, else -1
+    int32_t *chunk_row = nullptr; // per chunk: its row
+    int32_t nchunks = 0;
     bool unit = false;       // all |w| == 1
     bool integer = false;    // all integer-valued, small enough for int32 sums
     double wsum = 0;         // reference csr.sum
@@ -46,6 +53,7 @@ struct Work {
     int32_t *visits = nullptr;            // TSP streaming window scratch
     double2 *ab = nullptr;                // TSP (a_t, b_t) per step, FP64
     float2 *sched = nullptr;              // TSP (b_t, dt*-(1-a_t)) per step
+    uint32_t *part = nullptr;             // heavy-row partial counts
     unsigned long long *eacc = nullptr;   // per-agent cut accumulators
     double *cut = nullptr;                // per-agent cuts
     double *trace = nullptr;              // per-window best cut
@@ -56,7 +64,7 @@ struct Work {
     size_t cap_x = 0, cap_y = 0, cap_x2 = 0, cap_S0 = 0, cap_S1 = 0, cap_Wp = 0, cap_fin = 0,
            cap_chg = 0, cap_new = 0, cap_stab = 0, cap_bif = 0, cap_prev = 0, cap_ctl = 0,
            cap_win = 0, cap_visits = 0, cap_ab = 0, cap_sched = 0, cap_eacc = 0, cap_cut = 0,
-           cap_trace = 0, cap_tours = 0, cap_valid = 0, cap_rj = 0, cap_c32 = 0, cap_c64 = 0;
+           cap_trace = 0, cap_tours = 0, cap_valid = 0, cap_rj = 0, cap_c32 = 0, cap_c64 = 0, cap_part = 0;
 };
 
 // One solve's shape and scalars.

@@ -38,8 +38,11 @@ struct StepP {
     int32_t *ctl;
     const float4 *__restrict__ coef32;    // per step: k1, k2 (clamped p), k1, k2 (raw p)
     const Coef4 *__restrict__ coef64;
+    const int32_t *__restrict__ hchunk;   // heavy rows: first chunk, else -1
+    const int32_t *__restrict__ chunk_row;
+    uint2 *part;                          // [chunk][segment][lane] byte counters
     int64_t n;
-    int32_t W, Ap;
+    int32_t W, Ap, nchunks;
     double c0;
 };
 
@@ -91,6 +94,99 @@ template <class T, int V> __device__ __forceinline__ void vstore(T *p, const T (
 // hold 7 chunks of 32 neighbours; BIG rows (degree > 224) flush them into ints.
 // The new signs of the V agents are OR-combined across the lanes of a word
 // and written once.
+// Raw storage vector <-> arithmetic values.  16-bit types go two at a time
+// (one pack instruction per pair); the arithmetic is FP32.
+template <class T, int V, class A>
+__device__ __forceinline__ void to_vals(const Raw<V * sizeof(T)> &r, A (&o)[V])
+{
+    if constexpr (sizeof(T) == 2 && V >= 2) {
+        uint32_t w[V / 2];
+        memcpy(w, &r.u, sizeof w);
+#pragma unroll
+        for (int i = 0; i < V / 2; i++) {
+            if constexpr (std::is_same<T, __nv_bfloat16>::value) {
+                o[2 * i] = __uint_as_float(w[i] << 16);
+                o[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
+            } else {
+                const float2 f = __half22float2(*(const __half2 *)&w[i]);
+                o[2 * i] = f.x;
+                o[2 * i + 1] = f.y;
+            }
+        }
+    } else {
+        T t[V];
+        memcpy(t, &r.u, sizeof t);
+#pragma unroll
+        for (int v = 0; v < V; v++) o[v] = St<T>::ld(t[v]);
+    }
+}
+template <class T, int V, class A>
+__device__ __forceinline__ Raw<V * sizeof(T)> from_vals(const A (&o)[V])
+{
+    Raw<V * sizeof(T)> r;
+    if constexpr (sizeof(T) == 2 && V >= 2) {
+        uint32_t w[V / 2];
+#pragma unroll
+        for (int i = 0; i < V / 2; i++) {
+            if constexpr (std::is_same<T, __nv_bfloat16>::value) {
+                const __nv_bfloat162 h = __floats2bfloat162_rn(o[2 * i], o[2 * i + 1]);
+                w[i] = *(const uint32_t *)&h;
+            } else {
+                const __half2 h = __floats2half2_rn(o[2 * i], o[2 * i + 1]);
+                w[i] = *(const uint32_t *)&h;
+            }
+        }
+        memcpy(&r.u, w, sizeof w);
+    } else {
+        T t[V];
+#pragma unroll
+        for (int v = 0; v < V; v++) t[v] = St<T>::st(o[v]);
+        memcpy(&r.u, t, sizeof t);
+    }
+    return r;
+}
+
+// Partial counts of heavy rows (+-1 weights): item = (chunk of kHeavy
+// neighbours, segment of 32*V agents); a lane leaves the byte counters of its
+// V agents, which the step kernel then sums for the row.
+template <int V>
+__global__ void __launch_bounds__(256) k_heavy(const StepP P, const int offset)
+{
+    pdl_wait();
+    if (P.ctl[CTL_STOP]) return;
+    const int step = P.ctl[CTL_STEP] + offset;
+    pdl_trigger();
+    const int lane = threadIdx.x & 31;
+    const uint32_t *Scur = (step & 1) ? P.S1 : P.S0;
+    const int nit = P.Ap / (32 * V);
+    const int64_t items = (int64_t)P.nchunks * nit;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t item = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); item < items;
+         item += nw) {
+        const int c = (int)(item / nit), it = (int)(item - (int64_t)c * nit);
+        const int32_t r = __ldg(&P.chunk_row[c]);
+        const int32_t e0 = __ldg(&P.rowptr[r]) + (c - __ldg(&P.hchunk[r])) * kHeavy;
+        const int32_t e1 = min(__ldg(&P.rowptr[r + 1]), e0 + kHeavy);
+        const int a0 = it * 32 * V + lane * V;
+        const int q = a0 >> 5, off = a0 & 31;
+        const uint32_t *Sq = Scur + q;
+        uint32_t lo = 0, hi = 0;
+        for (int32_t cb = e0; cb < e1; cb += 32) {
+            const int m = min(32, e1 - cb);
+            const uint32_t mycw = lane < m ? __ldg(&P.colw[cb + lane]) : 0u;
+#pragma unroll 4
+            for (int k = 0; k < m; k++) {
+                const uint32_t cw = __shfl_sync(FULL, mycw, k);
+                uint32_t bits = __ldg(Sq + (size_t)(cw & 0x7fffffffu) * (size_t)P.W) >> off;
+                bits ^= (uint32_t)((int32_t)cw >> 31);
+                lo += spread4(bits & 0xfu);
+                if (V == 8) hi += spread4((bits >> 4) & 0xfu);
+            }
+        }
+        P.part[item * 32 + lane] = make_uint2(lo, hi);
+    }
+}
+
 // x + a*b: one FMA in FP32; in FP64 two separately rounded operations, the
 // reference's arithmetic as the oracle states it.
 __device__ __forceinline__ float madd(float a, float b, float x) { return fmaf(a, b, x); }
@@ -136,17 +232,14 @@ __global__ void __launch_bounds__(256) k_row(const StepP P, const int offset)
         const int64_t base = r * P.Ap + a0;
         const auto xr = vload<T, V>(xp + base);
         const auto yr = vload<T, V>(yp + base);
-        T xs[V], ys[V];
         A x[V], y[V];
         if (KIND == K_XY) {
             // Update_XY, src/kernels.cu:8-22 (pressure not clamped)
             const auto c = Coef<A>::get(P, step);
-            unpack<T, V>(xr, xs);
-            unpack<T, V>(yr, ys);
+            to_vals<T, V>(xr, x);
+            to_vals<T, V>(yr, y);
 #pragma unroll
             for (int v = 0; v < V; v++) {
-                x[v] = St<T>::ld(xs[v]);
-                y[v] = St<T>::ld(ys[v]);
                 y[v] = madd((A)c.w, x[v], y[v]);
                 x[v] = madd((A)c.z, y[v], x[v]);
             }
@@ -160,9 +253,10 @@ __global__ void __launch_bounds__(256) k_row(const StepP P, const int offset)
             for (int v = 0; v < (BIG ? V : 1); v++) cnt[v] = 0;
 #pragma unroll
             for (int v = 0; v < (WM == W_UNIT ? 1 : V); v++) tot[v] = R(0);
-            int chunk = 0;
-            for (int32_t cb = e0; cb < e1; cb += 32, chunk++) {
-                const int m = min(32, e1 - cb);
+            // heavy rows (BIG kernels only) take their counts from k_heavy
+            const int32_t e1w = (BIG && WM == W_UNIT && deg > kHeavy) ? e0 : e1;
+            for (int32_t cb = e0; cb < e1w; cb += 32) {
+                const int m = min(32, e1w - cb);
                 const uint32_t mycw = lane < m ? __ldg(&P.colw[cb + lane]) : 0u;
                 R myv = R(0);
                 if (WM == W_F32) myv = lane < m ? __ldg(&P.valf[cb + lane]) : 0.f;
@@ -190,45 +284,60 @@ __global__ void __launch_bounds__(256) k_row(const StepP P, const int offset)
                         }
                     }
                 }
-                if (BIG && WM == W_UNIT && (chunk % 7 == 6 || cb + 32 >= e1)) {
+            }
+            if (BIG && WM == W_UNIT) {
+                if (deg > kHeavy) {
+                    // a heavy row: its neighbours were counted in chunks by
+                    // k_heavy; the loop above did not run for it
+                    const int c0i = __ldg(&P.hchunk[r]), nc = (deg + kHeavy - 1) / kHeavy;
+                    for (int cc = 0; cc < nc; cc++) {
+                        const uint2 pr = P.part[((int64_t)(c0i + cc) * nit + it) * 32 + lane];
+#pragma unroll
+                        for (int v = 0; v < (BIG ? V : 1); v++)
+                            cnt[v] += ((v < 4 ? pr.x : pr.y) >> (8 * (v & 3))) & 0xffu;
+                    }
+                } else {
 #pragma unroll
                     for (int v = 0; v < (BIG ? V : 1); v++)
                         cnt[v] += ((v < 4 ? lo : hi) >> (8 * (v & 3))) & 0xffu;
-                    lo = hi = 0;
                 }
             }
             const auto c = Coef<A>::get(P, step);
             const A c0 = (A)P.c0;
-            unpack<T, V>(xr, xs);
-            unpack<T, V>(yr, ys);
+            // FP32 totals straight from the byte counters: PRMT builds the
+            // float 2^23 + count; fma(2, f, -2^24) is 2*count exactly, and
+            // subtracting the degree gives the exact integer 2*count - deg.
+            const float fdeg = (float)deg;
+            to_vals<T, V>(xr, x);
+            to_vals<T, V>(yr, y);
 #pragma unroll
             for (int v = 0; v < V; v++) {
-                x[v] = St<T>::ld(xs[v]);
-                y[v] = St<T>::ld(ys[v]);
-                int cv;
-                if (BIG) cv = cnt[v < (BIG ? V : 1) ? v : 0];
-                else cv = ((v < 4 ? lo : hi) >> (8 * (v & 3))) & 0xffu;
-                const A total = (WM == W_UNIT) ? (A)(2 * cv - deg) : (A)tot[WM == W_UNIT ? 0 : v];
+                A total;
+                if (WM != W_UNIT) {
+                    total = (A)tot[WM == W_UNIT ? 0 : v];
+                } else if (BIG) {
+                    total = (A)(2 * cnt[v < (BIG ? V : 1) ? v : 0] - deg);
+                } else if (std::is_same<A, float>::value) {
+                    const uint32_t f = __byte_perm(v < 4 ? lo : hi, 0x4b000000u, 0x7440u + (v & 3));
+                    total = (A)(fmaf(2.0f, __uint_as_float(f), -16777216.0f) - fdeg);
+                } else {
+                    total = (A)(2 * (int)(((v < 4 ? lo : hi) >> (8 * (v & 3))) & 0xffu) - deg);
+                }
+                const bool clamp = fabs(x[v]) > A(1);
+                const A xc = spin_of(x[v]);
                 if (KIND == K_FUSED) {
                     // src/kernels.cu:236-262: clamp or kick, then the drift /
                     // kick pair that runs unconditionally (a clamped oscillator
                     // leaves with y = dt (p-1) sign(x)).
-                    if (fabs(x[v]) > A(1)) {
-                        x[v] = spin_of(x[v]);
-                        y[v] = A(0);
-                    } else {
-                        y[v] = madd(c0, total, y[v]);
-                    }
+                    y[v] = clamp ? A(0) : madd(c0, total, y[v]);
+                    x[v] = clamp ? xc : x[v];
                     x[v] = madd((A)c.x, y[v], x[v]);
                     y[v] = madd((A)c.y, x[v], y[v]);
                 } else {
                     // mat_mult (:207) and confine (:158-165) of this step, then
                     // Update_XY of the next one unless the window closes here.
-                    y[v] = madd(c0, total, y[v]);
-                    if (fabs(x[v]) > A(1)) {
-                        x[v] = spin_of(x[v]);
-                        y[v] = A(0);
-                    }
+                    y[v] = clamp ? A(0) : madd(c0, total, y[v]);
+                    x[v] = clamp ? xc : x[v];
                     if (!WIN) {
                         const auto cn = Coef<A>::get(P, step + 1);
                         y[v] = madd((A)cn.w, x[v], y[v]);
@@ -237,15 +346,14 @@ __global__ void __launch_bounds__(256) k_row(const StepP P, const int offset)
                 }
             }
         }
+        // Signs of the new x (rounding to the storage type keeps the sign).
         uint32_t b = 0;
 #pragma unroll
-        for (int v = 0; v < V; v++) {
-            xs[v] = St<T>::st(x[v]);
-            ys[v] = St<T>::st(y[v]);
-            b |= sbit(St<T>::ld(xs[v])) << v;
-        }
-        vstore<T, V>(xp + base, xs);
-        vstore<T, V>(yp + base, ys);
+        for (int v = 0; v < V; v++) b |= sbit(x[v]) << v;
+        const auto xw = from_vals<T, V>(x);
+        const auto yw = from_vals<T, V>(y);
+        *(decltype(xw.u) *)(xp + base) = xw.u;
+        *(decltype(yw.u) *)(yp + base) = yw.u;
         b <<= off;
 #pragma unroll
         for (int sft = 1; sft < G; sft <<= 1) b |= __shfl_xor_sync(FULL, b, sft);
@@ -361,6 +469,10 @@ StepP make_step(const SolveDims &d, const DevCsr &J, Work &w)
     P.ctl = w.ctl;
     P.coef32 = (const float4 *)w.coef32;
     P.coef64 = (const Coef4 *)w.coef64;
+    P.hchunk = J.hchunk;
+    P.chunk_row = J.chunk_row;
+    P.part = (uint2 *)w.part;
+    P.nchunks = J.nchunks;
     P.n = d.n;
     P.W = d.W;
     P.Ap = d.Ap;
@@ -392,7 +504,11 @@ cudaError_t step_v(const SolveDims &d, const DevCsr &J, const StepP &P, int offs
 {
     const int64_t items = d.n * (d.Ap / (32 * V));
     const size_t smem = WIN ? sizeof(uint32_t) * d.W : 0;
-    const bool big = J.max_deg > 224;
+    const bool big = J.unit && J.nchunks > 0 && KIND != K_XY;
+    if (big) {
+        cudaError_t e = launch_grid(k_heavy<V>, d, (int64_t)J.nchunks * (d.Ap / (32 * V)), 0, s, P, offset);
+        if (e != cudaSuccess) return e;
+    }
     if (KIND == K_XY || J.unit) {
         if (big) return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, true>, d, items, smem, s, P, offset);
         return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, false>, d, items, smem, s, P, offset);

@@ -123,6 +123,57 @@ def test_fp64_first_steps_bitexact(ctx, oracle):
         np.testing.assert_array_equal(y, oy)
 
 
+def _hub_graph(n=2000, hub_deg=1500, seed=9):
+    """A ring plus two hubs (degrees above the 224-neighbour chunk), +-1 weights."""
+    rng = np.random.default_rng(seed)
+    edges = {(i, (i + 1) % n) if i < (i + 1) % n else ((i + 1) % n, i) for i in range(n)}
+    for hub in (0, 7):
+        for j in rng.choice(np.arange(10, n), size=hub_deg, replace=False):
+            a, b = min(hub, int(j)), max(hub, int(j))
+            if a != b:
+                edges.add((a, b))
+    edges = sorted(edges)
+    w = rng.choice([-1.0, 1.0], size=len(edges))
+    rows = np.array([e[0] for e in edges] + [e[1] for e in edges])
+    cols = np.array([e[1] for e in edges] + [e[0] for e in edges])
+    vals = np.concatenate([w, w])
+    order = np.lexsort((cols, rows))
+    rows, cols, vals = rows[order], cols[order], vals[order]
+    rowptr = np.zeros(n + 1, np.int64)
+    np.add.at(rowptr, rows + 1, 1)
+    return sbx.Graph(n, np.cumsum(rowptr), cols, vals, float(w.sum()))
+
+
+@pytest.mark.parametrize("fused", [1, 0])
+def test_fp64_heavy_rows_bitexact(ctx, oracle, fused):
+    # rows of degree > 224 go through the chunked partial-count kernel
+    g = _hub_graph()
+    assert np.diff(g.rowptr).max() > 1000
+    A, max_steps, dt, seed = 96, 3000, 0.3, 4
+    prob = ctx.problem(g)
+    r, cut = ctx.solve(prob, sbx.params(dt=dt, steps=max_steps, run_steps=200, agents=A,
+                                         fused=fused, seed=seed, precision=sbx.F64,
+                                         kernel=sbx.KERNEL_STREAM))
+    x, y, s = ctx.state(g.n, A)
+    og = _oracle_graph(oracle, g)
+    ox, oy = _oracle_first_steps(oracle, og, A, seed, dt, max_steps, 200, fused)
+    np.testing.assert_array_equal(x, ox)
+    np.testing.assert_array_equal(y, oy)
+    np.testing.assert_array_equal(oracle.cut(og, s, A), cut)
+
+
+@pytest.mark.parametrize("prec", [sbx.BF16, sbx.F32])
+def test_rmat_heavy_rows_cut_exact(ctx, oracle, prec):
+    g = sbx.gen_rmat(14, 4, seed=1234)
+    A = 256
+    prob = ctx.problem(g)
+    r, cut = ctx.solve(prob, sbx.params(dt=0.5, steps=300, agents=A, seed=3, precision=prec))
+    x, y, s = ctx.state(g.n, A)
+    og = _oracle_graph(oracle, g)
+    np.testing.assert_array_equal(oracle.cut(og, s, A), cut)
+    assert r["steps_run"] == 300
+
+
 @pytest.mark.parametrize("prec", [sbx.F32, sbx.BF16, sbx.F16])
 @pytest.mark.parametrize("kernel", [sbx.KERNEL_STREAM, sbx.KERNEL_RESIDENT])
 def test_cut_exact_and_close_to_fp64_on_torus(ctx, oracle, prec, kernel):
