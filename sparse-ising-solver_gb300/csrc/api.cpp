@@ -32,6 +32,19 @@ struct sbx_problem {
     DevTsp T;
 };
 
+// A class of batched instances sharing one padded agent count, packed into
+// one block-diagonal matrix.
+struct BatchClass {
+    std::vector<const sbx_problem *> probs;
+    std::vector<int> idx;                 // positions in the caller's batch
+    std::vector<int32_t> agents;
+    std::vector<int64_t> row_off;
+    std::vector<double> xi0, wsum;
+    int32_t Ap = 0;
+    DevCsr J;
+    double dt = -1;                       // dt of the uploaded per-row c0
+};
+
 struct sbx_ctx {
     int device = 0;
     cudaStream_t own = nullptr, stream = nullptr;
@@ -41,6 +54,7 @@ struct sbx_ctx {
     // graph cache for the streaming chunk
     cudaGraphExec_t gexec = nullptr;
     std::string gkey;
+    int gper_chunk = 0;
     std::vector<cudaEvent_t> prof;   // SBX_FLAG_PROFILE: events around step kernels
     // last solve
     bool have = false, last_tsp = false;
@@ -48,6 +62,8 @@ struct sbx_ctx {
     int32_t N = 0;
     std::string err;
     std::set<sbx_problem *> problems;   // live problems; orphaned on destroy
+    std::vector<BatchClass> batch;      // packed classes of the last batch
+    std::string batch_key;
 };
 
 namespace {
@@ -106,6 +122,12 @@ void free_csr(DevCsr &J)
     cudaFree(J.perm);
     cudaFree(J.hchunk);
     cudaFree(J.chunk_row);
+    cudaFree(J.c0r32);
+    cudaFree(J.c0r64);
+    cudaFree(J.rinst);
+    J.c0r32 = nullptr;
+    J.c0r64 = nullptr;
+    J.rinst = nullptr;
     J.hchunk = J.chunk_row = nullptr;
     J.nchunks = 0;
     J.rowptr = nullptr;
@@ -276,19 +298,49 @@ int ensure_common(sbx_ctx *ctx, const SolveDims &d, int64_t total_steps, int32_t
     return SBX_OK;
 }
 
+constexpr int64_t kRandChunk = 31 * 32;   // outputs per init thread
+constexpr int kRandBits = 40;             // jump matrices kept: 2^40 threads
+
+// x, y of one or more instances from their seeds' glibc rand() streams
+// (src/ising.cu:91-95, src/ising_tsp.cu:55-59), one launch.  Padded agents
+// and rows outside every instance are zero.
+int init_instances(sbx_ctx *ctx, const SolveDims &d, std::vector<RandInst> &inst, bool tsp)
+{
+    Work &w = ctx->w;
+    cudaStream_t s = ctx->stream;
+    if (!w.rjump_ready) {
+        std::vector<uint32_t> mats;
+        rand_jump_matrices(kRandChunk, kRandBits, mats);
+        CK(grow(w.rjump, w.cap_rj, mats.size()));
+        CK(cudaMemcpy(w.rjump, mats.data(), mats.size() * 4, cudaMemcpyHostToDevice));
+        w.rjump_ready = true;
+    }
+    int64_t threads = 0;
+    for (auto &I : inst) {
+        I.thread_base = threads;
+        const int64_t outputs = I.n * I.A * (tsp ? 1 : 2);
+        threads += (outputs + kRandChunk - 1) / kRandChunk;
+    }
+    const size_t es = prec_bytes(d.prec), nst = (size_t)d.n * d.Ap;
+    CK(cudaMemsetAsync(w.x, 0, nst * es, s));
+    CK(cudaMemsetAsync(w.y, 0, nst * es, s));
+    CK(grow(w.rinst, w.cap_rinst, inst.size()));
+    CK(cudaMemcpyAsync(w.rinst, inst.data(), sizeof(RandInst) * inst.size(), cudaMemcpyHostToDevice, s));
+    CK(launch_rand_init(d.prec, w.x, w.y, d.Ap, tsp, kRandChunk, w.rjump, w.rinst, (int)inst.size(),
+                        threads, s));
+    // the instance table must outlive the async copy
+    CK(cudaStreamSynchronize(s));
+    return SBX_OK;
+}
+
 int init_state(sbx_ctx *ctx, const SolveDims &d, uint32_t seed, bool tsp)
 {
-    const int64_t outputs = d.n * d.A * (tsp ? 1 : 2);
-    const int64_t L = 31 * 32;
-    const int nbits = rand_threads_bits(outputs, L);
-    std::vector<uint32_t> tab;
-    rand_jump_tables(seed, L, nbits, tab);
-    CK(grow(ctx->w.rjump, ctx->w.cap_rj, tab.size()));
-    CK(cudaMemcpyAsync(ctx->w.rjump, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-    CK(launch_rand_init(d, ctx->w, tsp, L, nbits, ctx->stream));
-    // the table must outlive the async copy
-    CK(cudaStreamSynchronize(ctx->stream));
-    return SBX_OK;
+    std::vector<RandInst> inst(1);
+    inst[0].row_off = 0;
+    inst[0].n = d.n;
+    inst[0].A = d.A;
+    rand_seed_window(seed, inst[0].V0);
+    return init_instances(ctx, d, inst, tsp);
 }
 
 int upload_coef(sbx_ctx *ctx, const SolveDims &d, int64_t total_steps)
@@ -321,6 +373,74 @@ bool poll_stop(sbx_ctx *ctx, int64_t c, bool force_all)
     if (old < 0) return false;
     cudaEventSynchronize(ctx->evp[old & 3]);
     return ctx->pinned[old & 3] != 0;
+}
+
+// The streaming loop of one solve: the pre-step Update_XY, then windows of
+// d.period steps (a captured CUDA graph per window, replayed), with the
+// all-bifurcated exit polled when d.uw.  Profile mode launches directly and
+// times every step kernel with events.
+int run_stream(sbx_ctx *ctx, const void *key_obj, const SolveDims &d, const DevCsr &J,
+               int64_t nchunks, bool profile, bool use_graph, int *launches_out, double *kernel_ms_out)
+{
+    cudaStream_t s = ctx->stream;
+    int launches = 0;
+    double kernel_ms = 0;
+    CK(launch_prestep(d, J, ctx->w, s, &launches));
+    if (nchunks) {
+        int per_chunk = 0;
+        if (use_graph) {
+            char key[256];
+            snprintf(key, sizeof key, "%p/%lld/%d/%d/%d/%d/%d/%d/%d/%d/%.17g/%llu/%p", key_obj,
+                     (long long)d.n, d.A, d.prec, d.period, d.fused, d.uw, d.threshold, (int)d.pdl,
+                     d.steps, d.c0, (unsigned long long)g_alloc_gen, (void *)s);
+            if (!ctx->gexec || ctx->gkey != key) {
+                if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+                ctx->gexec = nullptr;
+                cudaGraph_t g;
+                CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                cudaError_t e = launch_chunk(d, J, ctx->w, s, &per_chunk);
+                cudaError_t e2 = cudaStreamEndCapture(s, &g);
+                CK(e);
+                CK(e2);
+                CK(cudaGraphInstantiate(&ctx->gexec, g, 0));
+                cudaGraphDestroy(g);
+                ctx->gkey = key;
+                ctx->gper_chunk = per_chunk;
+            } else {
+                per_chunk = ctx->gper_chunk;
+            }
+            for (int64_t c = 0; c < nchunks; c++) {
+                CK(cudaGraphLaunch(ctx->gexec, s));
+                launches += per_chunk;
+                if (d.uw && poll_stop(ctx, c, false)) break;
+            }
+        } else {
+            cudaEvent_t *evs = nullptr;
+            if (profile) {
+                while ((int)ctx->prof.size() < 2 * d.period) {
+                    cudaEvent_t e;
+                    CK(cudaEventCreate(&e));
+                    ctx->prof.push_back(e);
+                }
+                evs = ctx->prof.data();
+            }
+            for (int64_t c = 0; c < nchunks; c++) {
+                CK(launch_chunk(d, J, ctx->w, s, &launches, evs));
+                if (profile) {
+                    CK(cudaStreamSynchronize(s));
+                    for (int i = 0; i < d.period; i++) {
+                        float t = 0;
+                        CK(cudaEventElapsedTime(&t, evs[2 * i], evs[2 * i + 1]));
+                        kernel_ms += t;
+                    }
+                }
+                if (d.uw && poll_stop(ctx, c, profile)) break;
+            }
+        }
+    }
+    *launches_out += launches;
+    *kernel_ms_out += kernel_ms;
+    return SBX_OK;
 }
 
 int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_result *res,
@@ -374,58 +494,8 @@ int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_r
             hot++;
         }
     } else {
-        CK(launch_prestep(d, p->J, ctx->w, s, &launches));
-        if (nchunks) {
-            int per_chunk = 0;
-            if (use_graph) {
-                char key[256];
-                snprintf(key, sizeof key, "%p/%lld/%d/%d/%d/%d/%d/%d/%d/%d/%.17g/%llu/%p", (void *)p,
-                         (long long)d.n, d.A, d.prec, d.period, d.fused, d.uw, d.threshold, (int)d.pdl,
-                         d.steps, d.c0, (unsigned long long)g_alloc_gen, (void *)s);
-                if (!ctx->gexec || ctx->gkey != key) {
-                    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
-                    ctx->gexec = nullptr;
-                    cudaGraph_t g;
-                    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-                    cudaError_t e = launch_chunk(d, p->J, ctx->w, s, &per_chunk);
-                    cudaError_t e2 = cudaStreamEndCapture(s, &g);
-                    CK(e);
-                    CK(e2);
-                    CK(cudaGraphInstantiate(&ctx->gexec, g, 0));
-                    cudaGraphDestroy(g);
-                    ctx->gkey = key;
-                } else {
-                    per_chunk = d.fused ? d.period + 2 : d.period + 3;
-                }
-                for (int64_t c = 0; c < nchunks; c++) {
-                    CK(cudaGraphLaunch(ctx->gexec, s));
-                    launches += per_chunk;
-                    if (d.uw && poll_stop(ctx, c, false)) break;
-                }
-            } else {
-                cudaEvent_t *evs = nullptr;
-                if (profile) {
-                    while ((int)ctx->prof.size() < 2 * d.period) {
-                        cudaEvent_t e;
-                        CK(cudaEventCreate(&e));
-                        ctx->prof.push_back(e);
-                    }
-                    evs = ctx->prof.data();
-                }
-                for (int64_t c = 0; c < nchunks; c++) {
-                    CK(launch_chunk(d, p->J, ctx->w, s, &launches, evs));
-                    if (profile) {
-                        CK(cudaStreamSynchronize(s));
-                        for (int i = 0; i < d.period; i++) {
-                            float t = 0;
-                            CK(cudaEventElapsedTime(&t, evs[2 * i], evs[2 * i + 1]));
-                            kernel_ms += t;
-                        }
-                    }
-                    if (d.uw && poll_stop(ctx, c, profile)) break;
-                }
-            }
-        }
+        if ((rc = run_stream(ctx, p, d, p->J, nchunks, profile, use_graph, &launches, &kernel_ms)))
+            return rc;
         hot = launches;
     }
     CK(cudaEventRecord(ctx->ev1, s));
@@ -599,6 +669,200 @@ int solve_tsp(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
     return SBX_OK;
 }
 
+
+// Pack the instances of one agent class into a block-diagonal matrix.
+int build_class(sbx_ctx *ctx, BatchClass &c)
+{
+    int64_t n = 0, nnz = 0;
+    for (const sbx_problem *p : c.probs) {
+        c.row_off.push_back(n);
+        n += p->J.n;
+        nnz += p->J.nnz;
+        c.xi0.push_back(xi0_of(p->J));
+        c.wsum.push_back(p->J.wsum);
+    }
+    if (n > INT32_MAX - 1 || nnz > INT32_MAX) return fail(ctx, SBX_ERR_UNSUPPORTED, "batch too large for int32 indices");
+    std::vector<int32_t> rp((size_t)n + 1), col((size_t)nnz), rinst((size_t)n);
+    std::vector<double> val((size_t)nnz);
+    int64_t e = 0;
+    for (size_t i = 0; i < c.probs.size(); i++) {
+        const DevCsr &J = c.probs[i]->J;
+        const int64_t r0 = c.row_off[i];
+        for (int64_t r = 0; r < J.n; r++) {
+            rp[r0 + r] = (int32_t)(e + J.hrowptr[r]);
+            rinst[r0 + r] = (int32_t)i;
+        }
+        for (int64_t k = 0; k < J.nnz; k++) {
+            col[e + k] = (int32_t)(J.hcol[k] + r0);
+            val[e + k] = J.hval[k];
+        }
+        e += J.nnz;
+    }
+    rp[n] = (int32_t)nnz;
+    int rc = upload_csr(ctx, c.J, n, nnz, rp.data(), col.data(), val.data(), 0.0);
+    if (rc) return rc;
+    CK(cudaMalloc(&c.J.rinst, sizeof(int32_t) * n));
+    CK(cudaMalloc(&c.J.c0r32, sizeof(float) * n));
+    CK(cudaMalloc(&c.J.c0r64, sizeof(double) * n));
+    CK(cudaMemcpy(c.J.rinst, rinst.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+    return SBX_OK;
+}
+
+// dt * xi0 of each row's instance (src/ising.cu:258 with the instance's xi0).
+int upload_c0(sbx_ctx *ctx, BatchClass &c, double dt)
+{
+    if (c.dt == dt) return SBX_OK;
+    std::vector<float> f((size_t)c.J.n);
+    std::vector<double> d((size_t)c.J.n);
+    for (size_t i = 0; i < c.probs.size(); i++) {
+        const double c0 = dt * c.xi0[i];
+        for (int64_t r = 0; r < c.probs[i]->J.n; r++) {
+            d[c.row_off[i] + r] = c0;
+            f[c.row_off[i] + r] = (float)c0;
+        }
+    }
+    CK(cudaMemcpy(c.J.c0r32, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c.J.c0r64, d.data(), sizeof(double) * d.size(), cudaMemcpyHostToDevice));
+    c.dt = dt;
+    return SBX_OK;
+}
+
+void free_batch(sbx_ctx *ctx)
+{
+    if (!ctx->batch.empty() && ctx->gexec) {   // a cached graph may point at a packed matrix
+        cudaGraphExecDestroy(ctx->gexec);
+        ctx->gexec = nullptr;
+        ctx->gkey.clear();
+    }
+    for (auto &c : ctx->batch) free_csr(c.J);
+    ctx->batch.clear();
+    ctx->batch_key.clear();
+}
+
+// Many MaxCut instances in one run per agent class: one block-diagonal
+// matrix, one init launch (each instance from its own seed, params.seed + its
+// position), the shared step kernels (the grid-stride row scheduler balances
+// instances of any size), and per-instance exact cuts and statistics.
+int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const int32_t *agents,
+                const sbx_params *pr, sbx_result *res, double *agent_values, double *batch_time_us)
+{
+    if (count < 1 || !problems || !agents || !pr || !res) return fail(ctx, SBX_ERR_ARG, "null argument");
+    if (pr->update_window)
+        return fail(ctx, SBX_ERR_UNSUPPORTED, "batched solve: update_window (per-instance exit) is not supported");
+    if (pr->steps < 0 || pr->precision < 0 || pr->precision > 3 || pr->run_steps < 0 || pr->period < 0)
+        return fail(ctx, SBX_ERR_ARG, "bad params");
+    std::string key;
+    for (int32_t i = 0; i < count; i++) {
+        const sbx_problem *p = problems[i];
+        if (!p || p->tsp || p->ctx != ctx) return fail(ctx, SBX_ERR_ARG, "batch: MaxCut problems of this context only");
+        if (agents[i] < 1) return fail(ctx, SBX_ERR_ARG, "batch: agents must be >= 1");
+        char b[64];
+        snprintf(b, sizeof b, "%p:%d;", (const void *)p, agents[i]);
+        key += b;
+    }
+    if (key != ctx->batch_key) {
+        free_batch(ctx);
+        std::vector<int32_t> aps;
+        for (int32_t i = 0; i < count; i++) {
+            const int32_t ap = (agents[i] + 31) / 32 * 32;
+            size_t k = 0;
+            while (k < aps.size() && aps[k] != ap) k++;
+            if (k == aps.size()) {
+                aps.push_back(ap);
+                ctx->batch.emplace_back();
+                ctx->batch.back().Ap = ap;
+            }
+            ctx->batch[k].probs.push_back(problems[i]);
+            ctx->batch[k].idx.push_back(i);
+            ctx->batch[k].agents.push_back(agents[i]);
+        }
+        for (auto &c : ctx->batch) {
+            int rc = build_class(ctx, c);
+            if (rc) {
+                free_batch(ctx);
+                return rc;
+            }
+        }
+        ctx->batch_key = key;
+    }
+    std::vector<int64_t> val_off((size_t)count + 1, 0);
+    for (int32_t i = 0; i < count; i++) val_off[i + 1] = val_off[i] + agents[i];
+    const bool profile = (pr->flags & SBX_FLAG_PROFILE) != 0;
+    const bool use_graph = !(pr->flags & SBX_FLAG_NO_GRAPH) && !profile;
+    cudaStream_t s = ctx->stream;
+    double total_us = 0;
+    for (auto &c : ctx->batch) {
+        if (!c.J.integer) return fail(ctx, SBX_ERR_UNSUPPORTED, "batched solve needs integer weights");
+        int rc = upload_c0(ctx, c, pr->dt);
+        if (rc) return rc;
+        SolveDims d;
+        d.n = c.J.n;
+        d.A = c.Ap;
+        d.Ap = c.Ap;
+        d.W = c.Ap / 32;
+        d.prec = pr->precision;
+        d.steps = pr->steps;
+        d.period = pr->period > 0 ? pr->period : 100;
+        d.threshold = pr->threshold > 0 ? pr->threshold : 25;
+        d.fused = pr->fused ? 1 : 0;
+        d.uw = 0;
+        d.dt = pr->dt;
+        d.pdl = !(pr->flags & SBX_FLAG_NO_PDL);
+        const int32_t run = pr->run_steps > 0 ? std::min(pr->run_steps, pr->steps) : pr->steps;
+        const int64_t nchunks = run > 0 ? (run + d.period - 1) / d.period : 0;
+        const int64_t total = nchunks * d.period;
+        if ((rc = ensure_common(ctx, d, total, c.J.nchunks))) return rc;
+        if ((rc = upload_coef(ctx, d, total))) return rc;
+        std::vector<RandInst> inst(c.probs.size());
+        for (size_t i = 0; i < c.probs.size(); i++) {
+            inst[i].row_off = c.row_off[i];
+            inst[i].n = c.probs[i]->J.n;
+            inst[i].A = c.agents[i];
+            rand_seed_window(pr->seed + (uint32_t)c.idx[i], inst[i].V0);
+        }
+        if ((rc = init_instances(ctx, d, inst, false))) return rc;
+        int launches = 0;
+        double kms = 0;
+        CK(cudaEventRecord(ctx->ev0, s));
+        if ((rc = run_stream(ctx, &c.J, d, c.J, nchunks, profile, use_graph, &launches, &kms))) return rc;
+        CK(cudaEventRecord(ctx->ev1, s));
+        const size_t ne = c.probs.size() * (size_t)c.Ap;
+        CK(grow(ctx->w.eacc, ctx->w.cap_eacc, ne));
+        CK(cudaMemsetAsync(ctx->w.eacc, 0, sizeof(unsigned long long) * ne, s));
+        CK(launch_cut_batch(d, c.J, ctx->w.Wp, ctx->w.eacc, s));
+        std::vector<long long> E(ne);
+        CK(cudaMemcpyAsync(E.data(), ctx->w.eacc, sizeof(long long) * ne, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        total_us += ms * 1000.0;
+        for (size_t i = 0; i < c.probs.size(); i++) {
+            const int gi = c.idx[i];
+            std::vector<double> cut((size_t)c.agents[i]);
+            for (int32_t a = 0; a < c.agents[i]; a++) {
+                // src/kernels.cu:383-398: -0.5 * (sum of halves - W), exact
+                const double tmp = 0.5 * (double)E[i * c.Ap + a];
+                cut[a] = -0.5 * (tmp - c.wsum[i]);
+            }
+            sbx_result *r = &res[gi];
+            memset(r, 0, sizeof *r);
+            stats(cut, r);
+            r->time_us = ms * 1000.0;
+            r->xi0 = c.xi0[i];
+            r->steps_run = total;
+            r->windows_run = nchunks;
+            r->kernel_used = SBX_KERNEL_STREAM;
+            r->kernel_launches = launches;
+            r->kernel_ms = kms;
+            r->gpu_launches = launches + 3;
+            if (agent_values) memcpy(agent_values + val_off[gi], cut.data(), sizeof(double) * c.agents[i]);
+        }
+    }
+    if (batch_time_us) *batch_time_us = total_us;
+    ctx->have = false;
+    return SBX_OK;
+}
+
 float bf16_to_f(uint16_t h)
 {
     uint32_t u = (uint32_t)h << 16;
@@ -704,7 +968,7 @@ int sbx_destroy(sbx_ctx *ctx)
     Work &w = ctx->w;
     void *ptrs[] = {w.x, w.y, w.x2, w.S[0], w.S[1], w.Wp, w.fin, w.chg, w.newmask, w.stab, w.bif,
                     w.prev, w.ctl, w.wincount, w.visits, w.ab, w.sched, w.eacc, w.cut, w.trace,
-                    w.tours, w.valid, w.rjump, w.coef32, w.coef64, w.part};
+                    w.tours, w.valid, w.rjump, w.coef32, w.coef64, w.part, w.rinst};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
@@ -715,6 +979,7 @@ int sbx_destroy(sbx_ctx *ctx)
     for (auto &e : ctx->prof) cudaEventDestroy(e);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->own) cudaStreamDestroy(ctx->own);
+    free_batch(ctx);
     for (sbx_problem *p : ctx->problems) p->ctx = nullptr;   // they stay valid to destroy
     delete ctx;
     return SBX_OK;
@@ -844,6 +1109,13 @@ int sbx_problem_destroy(sbx_problem *p)
     if (!p) return SBX_ERR_ARG;
     if (p->ctx) {
         p->ctx->problems.erase(p);
+        for (auto &c : p->ctx->batch)
+            for (const sbx_problem *q : c.probs)
+                if (q == p) {
+                    free_batch(p->ctx);   // the packed copy is stale
+                    goto freed;
+                }
+    freed:
         if (p->ctx->gexec) {   // a cached graph may point at this problem
             cudaGraphExecDestroy(p->ctx->gexec);
             p->ctx->gexec = nullptr;
@@ -946,14 +1218,9 @@ int sbx_get_tours(sbx_ctx *ctx, int32_t *tours, int32_t *valid_step)
 int sbx_solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const int32_t *agents,
                     const sbx_params *params, sbx_result *res, double *agent_values, double *batch_time_us)
 {
-    (void)count;
-    (void)problems;
-    (void)agents;
-    (void)params;
-    (void)res;
-    (void)agent_values;
-    (void)batch_time_us;
-    return fail(ctx, SBX_ERR_UNSUPPORTED, "batched solve not built yet");
+    if (!ctx) return fail(ctx, SBX_ERR_ARG, "null context");
+    CK(cudaSetDevice(ctx->device));
+    return solve_batch(ctx, count, problems, agents, params, res, agent_values, batch_time_us);
 }
 
 int sbx_get_trace(sbx_ctx *ctx, int64_t cap, int64_t *steps, double *best, int64_t *count)

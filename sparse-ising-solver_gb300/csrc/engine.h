@@ -11,6 +11,15 @@ namespace sbx {
 
 enum Prec { P_F32 = 0, P_BF16 = 1, P_F16 = 2, P_F64 = 3 };
 
+// One instance of the reference's init stream (k_init.cu): rows
+// [row_off, row_off + n) x agents [0, A) of x, y from srand(seed)'s window V0;
+// its device threads are thread_base .. thread_base + ceil(outputs/L) - 1.
+struct RandInst {
+    int64_t row_off, n, thread_base;
+    int32_t A, pad;
+    uint32_t V0[31];
+};
+
 constexpr int kHeavy = 224;   // neighbours per chunk: 7 x 32, byte counters never overflow
 
 inline size_t prec_bytes(int p) { return p == P_F64 ? 8 : p == P_F32 ? 4 : 2; }
@@ -30,6 +39,11 @@ struct DevCsr {
     int32_t *hchunk = nullptr;    // per row: first chunk of a heavy row, else -1
     int32_t *chunk_row = nullptr; // per chunk: its row
     int32_t nchunks = 0;
+    // Batched (block-diagonal) matrices: dt*xi0 of each row's instance, and
+    // the instance of each row; null for a single problem.
+    float *c0r32 = nullptr;
+    double *c0r64 = nullptr;
+    int32_t *rinst = nullptr;
     bool unit = false;       // all |w| == 1
     bool integer = false;    // all integer-valued, small enough for int32 sums
     double wsum = 0;         // reference csr.sum
@@ -58,13 +72,15 @@ struct Work {
     double *cut = nullptr;                // per-agent cuts
     double *trace = nullptr;              // per-window best cut
     int32_t *tours = nullptr, *valid = nullptr;
-    uint32_t *rjump = nullptr;            // rand jump tables
+    uint32_t *rjump = nullptr;            // rand jump matrices (computed once)
+    RandInst *rinst = nullptr;            // init instances of the current solve
     float *coef32 = nullptr;              // per-step coefficients (float4 / step)
     double *coef64 = nullptr;             // the same in FP64 (double4 / step)
     size_t cap_x = 0, cap_y = 0, cap_x2 = 0, cap_S0 = 0, cap_S1 = 0, cap_Wp = 0, cap_fin = 0,
            cap_chg = 0, cap_new = 0, cap_stab = 0, cap_bif = 0, cap_prev = 0, cap_ctl = 0,
            cap_win = 0, cap_visits = 0, cap_ab = 0, cap_sched = 0, cap_eacc = 0, cap_cut = 0,
-           cap_trace = 0, cap_tours = 0, cap_valid = 0, cap_rj = 0, cap_c32 = 0, cap_c64 = 0, cap_part = 0;
+           cap_trace = 0, cap_tours = 0, cap_valid = 0, cap_rj = 0, cap_c32 = 0, cap_c64 = 0, cap_part = 0, cap_rinst = 0;
+    bool rjump_ready = false;
 };
 
 // One solve's shape and scalars.
@@ -81,13 +97,14 @@ struct SolveDims {
 
 // ---- launchers (k_*.cu) ----
 
-// glibc rand() jump tables for `seed`: V0 (31 words) + nbits matrices of
-// 31x31, each M^(L*2^b).  Returns the words in `out`.
-void rand_jump_tables(uint32_t seed, int64_t L, int nbits, std::vector<uint32_t> &out);
+// glibc rand() on the device (k_init.cu).
+void rand_seed_window(uint32_t seed, uint32_t *V0);
+// out[b] = M^(L * 2^b), b < nbits (31x31 each): independent of the seed.
+void rand_jump_matrices(int64_t L, int nbits, std::vector<uint32_t> &out);
 int rand_threads_bits(int64_t outputs, int64_t L);
-// x, y <- the reference's init stream (tsp: x = 0, y from the stream).
-cudaError_t launch_rand_init(const SolveDims &d, Work &w, bool tsp, int64_t L, int nbits,
-                             cudaStream_t s);
+cudaError_t launch_rand_init(int prec, void *x, void *y, int32_t Ap, bool tsp, int64_t L,
+                             const uint32_t *mats, const RandInst *inst, int count,
+                             int64_t total_threads, cudaStream_t s);
 
 // Streaming MaxCut kernels (k_stream.cu).
 cudaError_t launch_prestep(const SolveDims &d, const DevCsr &J, Work &w, cudaStream_t s,
@@ -97,6 +114,9 @@ cudaError_t launch_chunk(const SolveDims &d, const DevCsr &J, Work &w, cudaStrea
                          int *launches, cudaEvent_t *evs = nullptr);
 cudaError_t launch_cut(const SolveDims &d, const DevCsr &J, Work &w, const uint32_t *plane,
                        cudaStream_t s, int *launches);
+// Integer weights, block-diagonal J: eacc[instance][Ap] += s_r sum_j J_rj s_j.
+cudaError_t launch_cut_batch(const SolveDims &d, const DevCsr &J, const uint32_t *plane,
+                             unsigned long long *eacc, cudaStream_t s);
 
 // Resident MaxCut kernel (k_resident.cu): returns cudaErrorInvalidValue when the
 // shape does not fit.

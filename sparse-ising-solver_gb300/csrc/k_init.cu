@@ -11,6 +11,8 @@
 // jumps to the start of its own chunk of outputs with precomputed powers
 // M^(L*2^b) and then runs the recurrence serially, so the whole stream is
 // produced in parallel and equals, value for value, what rand() returns.
+// The powers do not depend on the seed; one launch can fill many instances,
+// each from its own seed (its own 31-word starting window).
 #include "common.cuh"
 #include "engine.h"
 
@@ -36,10 +38,10 @@ void matmul31(const uint32_t *a, const uint32_t *b, uint32_t *c)
 
 }  // namespace
 
-void rand_jump_tables(uint32_t seed, int64_t L, int nbits, std::vector<uint32_t> &out)
+void rand_seed_window(uint32_t seed, uint32_t *V0)
 {
-    // Seeding: the minimal-standard LCG, then the lag-31 recurrence up to the
-    // first returned value.
+    // the minimal-standard LCG, then the lag-31 recurrence up to the first
+    // returned value; V0 = u[313..343], the window before output 0
     uint32_t u[344];
     uint64_t word = seed ? seed : 1u;
     u[0] = (uint32_t)word;
@@ -49,22 +51,25 @@ void rand_jump_tables(uint32_t seed, int64_t L, int nbits, std::vector<uint32_t>
     }
     for (int i = 31; i < 34; i++) u[i] = u[i - 31];
     for (int i = 34; i < 344; i++) u[i] = u[i - 31] + u[i - 3];
-    out.assign(R + (size_t)nbits * R * R, 0);
-    for (int i = 0; i < R; i++) out[i] = u[313 + i];   // window before output 0
-    // M: window (u[i-31..i-1]) -> (u[i-30..i]).
+    for (int i = 0; i < R; i++) V0[i] = u[313 + i];
+}
+
+void rand_jump_matrices(int64_t L, int nbits, std::vector<uint32_t> &out)
+{
+    // M: window (u[i-31..i-1]) -> (u[i-30..i]); out[b] = M^(L*2^b)
     uint32_t M[R * R] = {0}, P[R * R], Acc[R * R];
     for (int i = 0; i < R - 1; i++) M[i * R + i + 1] = 1;
     M[(R - 1) * R + 0] = 1;
     M[(R - 1) * R + 28] = 1;
-    // P = M^L by square-and-multiply.
     for (int i = 0; i < R * R; i++) Acc[i] = (i % (R + 1)) == 0;
     memcpy(P, M, sizeof P);
     for (int64_t e = L; e; e >>= 1) {
         if (e & 1) matmul31(Acc, P, Acc);
         matmul31(P, P, P);
     }
+    out.assign((size_t)nbits * R * R, 0);
     for (int b = 0; b < nbits; b++) {
-        memcpy(&out[R + (size_t)b * R * R], Acc, sizeof Acc);
+        memcpy(&out[(size_t)b * R * R], Acc, sizeof Acc);
         matmul31(Acc, Acc, Acc);
     }
 }
@@ -82,21 +87,32 @@ namespace {
 template <class T>
 __device__ __forceinline__ void put(T *p, int64_t i, double v) { p[i] = St<T>::st((typename St<T>::A)v); }
 
-// One thread: jump to output t*L, then emit L outputs.
+// One thread: find its instance, jump to its chunk start, emit L outputs.
 template <class T>
-__global__ void __launch_bounds__(128) k_rand_init(T *x, T *y, int64_t outputs, int32_t A,
-                                                   int32_t Ap, int tsp, int64_t L, int nbits,
-                                                   const uint32_t *__restrict__ tab)
+__global__ void __launch_bounds__(128) k_rand_init(T *x, T *y, int32_t Ap, int tsp, int64_t L,
+                                                   const uint32_t *__restrict__ mats,
+                                                   const RandInst *__restrict__ inst, int count,
+                                                   int64_t total_threads)
 {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t o0 = t * L;
+    if (t >= total_threads) return;
+    int lo = 0, hi = count - 1;   // last instance with thread_base <= t
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (inst[mid].thread_base <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    const RandInst &I = inst[lo];
+    const int64_t lt = t - I.thread_base;
+    const int64_t outputs = I.n * I.A * (tsp ? 1 : 2);
+    const int64_t o0 = lt * L;
     if (o0 >= outputs) return;
     uint32_t v[R];
 #pragma unroll
-    for (int i = 0; i < R; i++) v[i] = __ldg(&tab[i]);
-    for (int b = 0; b < nbits; b++) {
-        if (!((t >> b) & 1)) continue;
-        const uint32_t *P = tab + R + (size_t)b * R * R;
+    for (int i = 0; i < R; i++) v[i] = I.V0[i];
+    for (int b = 0; (lt >> b) != 0; b++) {
+        if (!((lt >> b) & 1)) continue;
+        const uint32_t *P = mats + (size_t)b * R * R;
         uint32_t nv[R];
 #pragma unroll
         for (int i = 0; i < R; i++) {
@@ -109,12 +125,14 @@ __global__ void __launch_bounds__(128) k_rand_init(T *x, T *y, int64_t outputs, 
         for (int i = 0; i < R; i++) v[i] = nv[i];
     }
     const int64_t o1 = min(o0 + L, outputs);
+    const int64_t A = I.A;
+    T *xi = x + I.row_off * Ap, *yi = y + I.row_off * Ap;
     int64_t o = o0;
     // Circular window: at phase q, v[q] holds u[i-31] and v[(q+28)%31] u[i-3].
     while (o < o1) {
 #pragma unroll
         for (int q = 0; q < R; q++) {
-            uint32_t nu = v[q] + v[(q + 28) % R];
+            const uint32_t nu = v[q] + v[(q + 28) % R];
             v[q] = nu;
             if (o < o1) {
                 const double r = (double)(nu >> 1);
@@ -122,13 +140,13 @@ __global__ void __launch_bounds__(128) k_rand_init(T *x, T *y, int64_t outputs, 
                 const double val =
                     __ddiv_rn(__dsub_rn(__dmul_rn(__ddiv_rn(r, 2147483647.0), 2.0), 1.0), 10.0);
                 if (tsp) {
-                    const int64_t e = o, row = e / A, a = e - row * A, idx = row * Ap + a;
-                    put(x, idx, 0.0);
-                    put(y, idx, val);
+                    const int64_t row = o / A, a = o - row * A, idx = row * Ap + a;
+                    put(xi, idx, 0.0);
+                    put(yi, idx, val);
                 } else {
                     const int64_t e = o >> 1, row = e / A, a = e - row * A, idx = row * Ap + a;
-                    if (o & 1) put(y, idx, val);
-                    else put(x, idx, val);
+                    if (o & 1) put(yi, idx, val);
+                    else put(xi, idx, val);
                 }
             }
             o++;
@@ -137,34 +155,28 @@ __global__ void __launch_bounds__(128) k_rand_init(T *x, T *y, int64_t outputs, 
 }
 
 template <class T>
-cudaError_t launch_t(const SolveDims &d, Work &w, bool tsp, int64_t L, int nbits,
-                     cudaStream_t s)
+cudaError_t launch_t(void *x, void *y, int32_t Ap, int tsp, int64_t L, const uint32_t *mats,
+                     const RandInst *inst, int count, int64_t total_threads, cudaStream_t s)
 {
-    const int64_t outputs = d.n * d.A * (tsp ? 1 : 2);
-    const int64_t threads = (outputs + L - 1) / L;
     const int blk = 128;
-    const int64_t grid = (threads + blk - 1) / blk;
-    // padded agents start (and stay) at zero
-    if (d.Ap != d.A) {
-        cudaError_t e = cudaMemsetAsync(w.x, 0, (size_t)d.n * d.Ap * sizeof(T), s);
-        if (e == cudaSuccess) e = cudaMemsetAsync(w.y, 0, (size_t)d.n * d.Ap * sizeof(T), s);
-        if (e != cudaSuccess) return e;
-    }
-    k_rand_init<T><<<(unsigned)grid, blk, 0, s>>>((T *)w.x, (T *)w.y, outputs, d.A, d.Ap,
-                                                 tsp ? 1 : 0, L, nbits, w.rjump);
+    const int64_t grid = (total_threads + blk - 1) / blk;
+    if (grid == 0) return cudaSuccess;
+    k_rand_init<T><<<(unsigned)grid, blk, 0, s>>>((T *)x, (T *)y, Ap, tsp, L, mats, inst, count,
+                                                 total_threads);
     return cudaGetLastError();
 }
 
 }  // namespace
 
-cudaError_t launch_rand_init(const SolveDims &d, Work &w, bool tsp, int64_t L, int nbits,
-                             cudaStream_t s)
+cudaError_t launch_rand_init(int prec, void *x, void *y, int32_t Ap, bool tsp, int64_t L,
+                             const uint32_t *mats, const RandInst *inst, int count,
+                             int64_t total_threads, cudaStream_t s)
 {
-    switch (d.prec) {
-    case P_F32: return launch_t<float>(d, w, tsp, L, nbits, s);
-    case P_BF16: return launch_t<__nv_bfloat16>(d, w, tsp, L, nbits, s);
-    case P_F16: return launch_t<__half>(d, w, tsp, L, nbits, s);
-    default: return launch_t<double>(d, w, tsp, L, nbits, s);
+    switch (prec) {
+    case P_F32: return launch_t<float>(x, y, Ap, tsp, L, mats, inst, count, total_threads, s);
+    case P_BF16: return launch_t<__nv_bfloat16>(x, y, Ap, tsp, L, mats, inst, count, total_threads, s);
+    case P_F16: return launch_t<__half>(x, y, Ap, tsp, L, mats, inst, count, total_threads, s);
+    default: return launch_t<double>(x, y, Ap, tsp, L, mats, inst, count, total_threads, s);
     }
 }
 

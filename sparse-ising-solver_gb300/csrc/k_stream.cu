@@ -41,6 +41,8 @@ struct StepP {
     const int32_t *__restrict__ hchunk;   // heavy rows: first chunk, else -1
     const int32_t *__restrict__ chunk_row;
     uint2 *part;                          // [chunk][segment][lane] byte counters
+    const float *__restrict__ c0r32;      // batched: dt*xi0 per row (else null)
+    const double *__restrict__ c0r64;
     int64_t n;
     int32_t W, Ap, nchunks;
     double c0;
@@ -303,7 +305,8 @@ __global__ void __launch_bounds__(256) k_row(const StepP P, const int offset)
                 }
             }
             const auto c = Coef<A>::get(P, step);
-            const A c0 = (A)P.c0;
+            A c0 = (A)P.c0;
+            if (P.c0r32) c0 = std::is_same<A, double>::value ? (A)__ldg(&P.c0r64[r]) : (A)__ldg(&P.c0r32[r]);
             // FP32 totals straight from the byte counters: PRMT builds the
             // float 2^23 + count; fma(2, f, -2^24) is 2*count exactly, and
             // subtracting the degree gives the exact integer 2*count - deg.
@@ -473,6 +476,8 @@ StepP make_step(const SolveDims &d, const DevCsr &J, Work &w)
     P.chunk_row = J.chunk_row;
     P.part = (uint2 *)w.part;
     P.nchunks = J.nchunks;
+    P.c0r32 = J.c0r32;
+    P.c0r64 = J.c0r64;
     P.n = d.n;
     P.W = d.W;
     P.Ap = d.Ap;
@@ -588,7 +593,8 @@ cudaError_t launch_chunk(const SolveDims &d, const DevCsr &J, Work &w, cudaStrea
         e = step(d, J, P, d.fused ? K_FUSED : K_FC, i == d.period - 1, i, s);
         if (evs) cudaEventRecord(evs[2 * i + 1], s);
     }
-    *launches += d.period;
+    // heavy-row partial counts: one more launch per step
+    *launches += d.period * ((J.unit && J.nchunks > 0) ? 2 : 1);
     if (e != cudaSuccess) return e;
     WinP Q;
     Q.chg = w.chg;
@@ -651,6 +657,42 @@ __global__ void __launch_bounds__(256) k_cut_int(const int32_t *__restrict__ row
     }
 }
 
+// Block-diagonal (batched) matrices: as k_cut_int, but each row adds into its
+// instance's accumulators; a warp flushes when its rows change instance.
+__global__ void __launch_bounds__(256) k_cut_batch(const int32_t *__restrict__ rowptr,
+                                                   const uint32_t *__restrict__ colw,
+                                                   const float *__restrict__ valf, int unit,
+                                                   const uint32_t *__restrict__ plane, int64_t n,
+                                                   int32_t W, int32_t Ap,
+                                                   const int32_t *__restrict__ rinst,
+                                                   int64_t rows_per_block, unsigned long long *eacc)
+{
+    const int w = blockIdx.y, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t r0 = (int64_t)blockIdx.x * rows_per_block;
+    const int64_t r1 = min(n, r0 + rows_per_block);
+    long long acc = 0;
+    int cur = -1;
+    for (int64_t r = r0 + warp; r < r1; r += 8) {
+        const int inst = rinst[r];
+        if (inst != cur) {
+            if (cur >= 0 && acc) atomicAdd(&eacc[(int64_t)cur * Ap + w * 32 + lane], (unsigned long long)acc);
+            acc = 0;
+            cur = inst;
+        }
+        long long t = 0;
+        for (int32_t e = rowptr[r]; e < rowptr[r + 1]; e++) {
+            const uint32_t cw = colw[e];
+            const uint32_t word = plane[(int64_t)(cw & 0x7fffffffu) * W + w];
+            const int neg = (word >> lane) & 1u;
+            if (unit) t += (((uint32_t)neg ^ (cw >> 31)) & 1u) ? -1 : 1;
+            else t += neg ? -(long long)valf[e] : (long long)valf[e];
+        }
+        const int sr = (plane[r * W + w] >> lane) & 1u;
+        acc += sr ? -t : t;
+    }
+    if (cur >= 0 && acc) atomicAdd(&eacc[(int64_t)cur * Ap + w * 32 + lane], (unsigned long long)acc);
+}
+
 __global__ void k_cut_finish(const unsigned long long *eacc, int32_t A, double wsum, double *cut)
 {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
@@ -683,6 +725,16 @@ __global__ void k_cut_ordered(const int32_t *__restrict__ rowptr, const uint32_t
 }
 
 }  // namespace
+
+cudaError_t launch_cut_batch(const SolveDims &d, const DevCsr &J, const uint32_t *plane,
+                             unsigned long long *eacc, cudaStream_t s)
+{
+    const int64_t rpb = 256;
+    const dim3 grid((unsigned)((d.n + rpb - 1) / rpb), (unsigned)d.W);
+    k_cut_batch<<<grid, 256, 0, s>>>(J.rowptr, J.colw, J.valf, J.unit ? 1 : 0, plane, d.n, d.W, d.Ap,
+                                     J.rinst, rpb, eacc);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_cut(const SolveDims &d, const DevCsr &J, Work &w, const uint32_t *plane,
                        cudaStream_t s, int *launches)

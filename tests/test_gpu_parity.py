@@ -325,3 +325,28 @@ def test_tsp_config_shape_runs_and_decodes(ctx, oracle):
             assert sorted(tours[a].tolist()) == list(range(30))
             assert lengths[a] == t.tour_length(tours[a])
     assert nvalid == r["valid"]
+
+
+def _batch_instances():
+    gs = [sbx.gen_er(300, 0.04, pm1=True, seed=1), sbx.gen_rgg(900, 8.0, seed=2),
+          sbx.gen_torus(20, 30, seed=3), _hub_graph(1200, 400, seed=4),
+          sbx.gen_er(150, 0.1, pm1=False, seed=5)]
+    agents = [64, 64, 40, 64, 96]
+    return gs, agents
+
+
+@pytest.mark.parametrize("prec", [sbx.F64, sbx.BF16])
+def test_batch_matches_single_solves(ctx, prec):
+    # Each instance of a batch behaves exactly as solved alone from seed + i:
+    # same per-agent cuts (bit-exact), at FP64 and at BF16.
+    gs, agents = _batch_instances()
+    probs = [ctx.problem(g) for g in gs]
+    base = dict(dt=0.5, steps=700, seed=100, precision=prec, kernel=sbx.KERNEL_STREAM)
+    res, vals, t_us = ctx.solve_batch(probs, agents, sbx.params(**base))
+    off = 0
+    for i, (p, a) in enumerate(zip(probs, agents)):
+        r1, cut1 = ctx.solve(p, sbx.params(agents=a, **dict(base, seed=100 + i)))
+        np.testing.assert_array_equal(vals[off:off + a], cut1)
+        assert res[i]["max"] == r1["max"] and res[i]["xi0"] == r1["xi0"]
+        off += a
+    assert t_us > 0
