@@ -182,6 +182,7 @@ int upload_csr(sbx_ctx *ctx, DevCsr &J, int64_t n, int64_t nnz, const int32_t *r
     J.integer = integer;
     J.wsum = wsum;
     J.max_deg = maxdeg;
+    J.skewed = (double)maxdeg > 8.0 * std::max(1.0, (double)nnz / (double)n);
     J.hval.assign(val, val + nnz);
     J.hrowptr.assign(rowptr, rowptr + n + 1);
     J.hcol.assign(col, col + nnz);

@@ -20,7 +20,9 @@ struct RandInst {
     uint32_t V0[31];
 };
 
-constexpr int kHeavy = 224;   // neighbours per chunk: 7 x 32, byte counters never overflow
+// Rows with more neighbours than this are "heavy" (+-1 weights): a separate
+// kernel counts them in chunks of kHeavy; byte counters never overflow.
+constexpr int kHeavy = 128;
 
 inline size_t prec_bytes(int p) { return p == P_F64 ? 8 : p == P_F32 ? 4 : 2; }
 
@@ -34,6 +36,7 @@ struct DevCsr {
     double *vald = nullptr;
     float *valf = nullptr;
     int32_t *perm = nullptr; // rows in decreasing degree (resident kernel order)
+    bool skewed = false;     // max degree > 8x mean: the step kernel visits rows in perm order
     // Heavy rows (unit weights, degree > kHeavy) are split into chunks of
     // kHeavy neighbours whose partial counts a separate kernel computes.
     int32_t *hchunk = nullptr;    // per row: first chunk of a heavy row, else -1

@@ -41,6 +41,7 @@ struct StepP {
     const int32_t *__restrict__ hchunk;   // heavy rows: first chunk, else -1
     const int32_t *__restrict__ chunk_row;
     uint2 *part;                          // [chunk][segment][lane] byte counters
+    const int32_t *__restrict__ order;    // skewed graphs: rows in decreasing degree
     const float *__restrict__ c0r32;      // batched: dt*xi0 per row (else null)
     const double *__restrict__ c0r64;
     int64_t n;
@@ -92,8 +93,9 @@ template <class T, int V> __device__ __forceinline__ void vstore(T *p, const T (
 // sign word of its agents in row j of the plane (lanes of one word share the
 // address), XORs the weight's sign and adds the V bits into byte counters
 // (bit i of a nibble lands in byte i after multiplying by 0x00204081); the
-// force is 2*count - degree, exact (src/kernels.cu:247-255).  Byte counters
-// hold 7 chunks of 32 neighbours; BIG rows (degree > 224) flush them into ints.
+// force is 2*count - degree, exact (src/kernels.cu:247-255).  A byte counter
+// holds up to kHeavy = 128 neighbours; longer rows (+-1 weights) are counted
+// in kHeavy chunks by k_heavy and the BIG kernels add those partials.
 // The new signs of the V agents are OR-combined across the lanes of a word
 // and written once.
 // Raw storage vector <-> arithmetic values.  16-bit types go two at a time
@@ -221,17 +223,22 @@ __global__ void __launch_bounds__(256) k_row(const StepP P, const int offset)
     const int64_t w0 = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int64_t dr = nw / nit;
     const int dit = (int)(nw - dr * nit);
-    int64_t r = w0 / nit;
-    int it = (int)(w0 - r * nit);
-    for (; r < P.n; r += dr, it += dit) {
+    // Skewed graphs are visited in decreasing degree, so every warp's share
+    // holds the same mix of long and short rows.
+    int64_t ri = w0 / nit;
+    int it = (int)(w0 - ri * nit);
+    for (; ri < P.n; ri += dr, it += dit) {
         if (it >= nit) {
             it -= nit;
-            r++;
-            if (r >= P.n) break;
+            ri++;
+            if (ri >= P.n) break;
         }
+        const int64_t r = P.order ? (int64_t)__ldg(&P.order[ri]) : ri;
         const int a0 = it * 32 * V + lane * V;
         const int q = a0 >> 5, off = a0 & 31;
         const int64_t base = r * P.Ap + a0;
+        uint32_t wp_old = 0;   // window steps: the previous window's word, fetched early
+        if (WIN && (lane & (G - 1)) == 0) wp_old = P.Wp[r * P.W + q];
         const auto xr = vload<T, V>(xp + base);
         const auto yr = vload<T, V>(yp + base);
         A x[V], y[V];
@@ -366,7 +373,7 @@ __global__ void __launch_bounds__(256) k_row(const StepP P, const int offset)
             else if (KIND == K_FUSED || !WIN) Snext[wi] = b;
             if (WIN) {
                 // window compare, src/kernels.cu:37-46 + :84-90
-                const uint32_t ch = b ^ P.Wp[wi];
+                const uint32_t ch = b ^ wp_old;
                 P.Wp[wi] = b;
                 if (ch) atomicOr(&s_chg[q], ch);
             }
@@ -476,6 +483,7 @@ StepP make_step(const SolveDims &d, const DevCsr &J, Work &w)
     P.chunk_row = J.chunk_row;
     P.part = (uint2 *)w.part;
     P.nchunks = J.nchunks;
+    P.order = J.skewed ? J.perm : nullptr;
     P.c0r32 = J.c0r32;
     P.c0r64 = J.c0r64;
     P.n = d.n;
