@@ -49,6 +49,7 @@ enum { SBX_DIST_EUC_2D = 0, SBX_DIST_GEO = 1, SBX_DIST_EUC_2D_FLOAT = 2 };
 #define SBX_FLAG_NO_PDL 1u      /* launch without programmatic dependent launch */
 #define SBX_FLAG_NO_GRAPH 2u    /* launch kernels directly, not through a graph */
 #define SBX_FLAG_PROFILE 4u     /* time every hot-kernel launch with events */
+#define SBX_FLAG_NO_TUNE 8u     /* streaming tile from the fixed heuristic, not timed */
 
 typedef struct sbx_ctx sbx_ctx;
 typedef struct sbx_problem sbx_problem;
@@ -69,6 +70,15 @@ typedef struct sbx_params {
     uint32_t flags;         /* SBX_FLAG_* */
     int32_t run_steps;      /* run only the first run_steps steps of the
                                schedule set by `steps` (0: all of them) */
+    /* Streaming step tile; 0 leaves the field to the autotuner, which times
+     * the candidate tiles on the problem once and caches the fastest.  Every
+     * tile computes identical results. */
+    int32_t lane_agents;    /* agents per lane: 1, 2, 4 or 8 (16-bit states) */
+    int32_t row_lanes;      /* lanes per row: 32, or 16/8/4 (several rows per
+                               warp; then lane_agents * row_lanes = padded agents) */
+    int32_t block_threads;  /* threads per CTA: 128 or 256 */
+    double target;          /* MaxCut: a cut; > 0 records the per-window best
+                               cut (as trace = 1) and times its first reach */
 } sbx_params;
 
 typedef struct sbx_result {
@@ -83,10 +93,16 @@ typedef struct sbx_result {
     int32_t best_agent;     /* first agent reaching max (MaxCut) / min (TSP) */
     int32_t kernel_used;    /* SBX_KERNEL_STREAM or SBX_KERNEL_RESIDENT */
     int32_t agents_per_block;
-    int32_t reserved;
+    int32_t lane_agents;    /* streaming tile used (0 for other kernels) */
+    int32_t row_lanes;
+    int32_t block_threads;
     double kernel_ms;       /* SBX_FLAG_PROFILE: summed hot-kernel time */
     int64_t kernel_launches;/* hot-kernel launches issued by the solve */
     int64_t gpu_launches;   /* all kernel launches issued by the solve */
+    double time_to_target_us; /* params.target: first window whose best cut
+                                 reaches it, microseconds after the SB loop
+                                 began (device clock); -1 if never */
+    int64_t steps_to_target;  /* SB steps run at that window; -1 if never */
 } sbx_result;
 
 const char *sbx_strerror(int status);
@@ -126,9 +142,12 @@ int sbx_get_state(sbx_ctx *ctx, double *x, double *y, int32_t *spins);
 /* TSP tours of the last solve: tours[agents*N] (city order, -1 when the agent
  * has no valid tour) and valid_step[agents] (ising_tsp.cu valid_list). */
 int sbx_get_tours(sbx_ctx *ctx, int32_t *tours, int32_t *valid_step);
-/* Best cut after each window of the last solve (params.trace = 1). */
+/* Per-window record of the last MaxCut solve run with params.trace = 1 or
+ * params.target > 0: SB steps run, best cut over agents of the window spins,
+ * and microseconds since the SB loop began (device clock).  Up to cap entries
+ * are written; *count receives the number recorded.  NULL arrays skip. */
 int sbx_get_trace(sbx_ctx *ctx, int64_t cap, int64_t *steps, double *best,
-                  int64_t *count);
+                  double *t_us, int64_t *count);
 
 /* ---- batched MaxCut: many independent instances, one launch per step ---- */
 /* Each instance keeps its own xi0, weight sum and agent count; all share

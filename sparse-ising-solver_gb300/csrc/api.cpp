@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstring>
 #include <numeric>
+#include <map>
 #include <set>
 #include <string>
 #include <vector>
@@ -25,11 +26,17 @@
 
 using namespace sbx;
 
+// Streaming step tile (agents per lane, lanes per row, threads per CTA).
+struct Tile {
+    int32_t v = 0, lr = 32, bt = 256;
+};
+
 struct sbx_problem {
     sbx_ctx *ctx = nullptr;
     bool tsp = false;
     DevCsr J;
     DevTsp T;
+    mutable std::map<std::string, Tile> tiles;   // autotuned tiles by precision/agents/mode
 };
 
 // A class of batched instances sharing one padded agent count, packed into
@@ -43,6 +50,7 @@ struct BatchClass {
     int32_t Ap = 0;
     DevCsr J;
     double dt = -1;                       // dt of the uploaded per-row c0
+    std::map<std::string, Tile> tiles;
 };
 
 struct sbx_ctx {
@@ -64,6 +72,7 @@ struct sbx_ctx {
     std::set<sbx_problem *> problems;   // live problems; orphaned on destroy
     std::vector<BatchClass> batch;      // packed classes of the last batch
     std::string batch_key;
+    std::vector<TraceRec> trace;        // per-window records of the last traced solve
 };
 
 namespace {
@@ -284,6 +293,10 @@ int ensure_common(sbx_ctx *ctx, const SolveDims &d, int64_t total_steps, int32_t
     CK(grow(w.wincount, w.cap_win, (size_t)nwin));
     CK(grow(w.coef32, w.cap_c32, (size_t)(total_steps + 2) * 4));
     CK(grow(w.coef64, w.cap_c64, (size_t)(total_steps + 2) * 4));
+    if (d.trace) {
+        CK(grow(w.trace, w.cap_trace, (size_t)nwin));
+        CK(grow(w.trace_t0, w.cap_t0, (size_t)1));
+    }
     cudaStream_t s = ctx->stream;
     CK(cudaMemsetAsync(w.Wp, 0xff, npl * 4, s));   // current_spins = -1 (ising.cu:128)
     CK(cudaMemsetAsync(w.fin, 0xff, npl * 4, s));  // final_spins = -1 (ising.cu:129)
@@ -376,6 +389,124 @@ bool poll_stop(sbx_ctx *ctx, int64_t c, bool force_all)
     return ctx->pinned[old & 3] != 0;
 }
 
+// ---- streaming step tile
+
+// A tile the step kernels are built for (k_step.cuh, step_kw): whole-warp
+// rows take any vector width dividing the padded agents; 16, 8 or 4 lanes
+// per row take the two widest vectors and exactly the padded agents, and
+// rows with split heavy neighbour lists need whole-warp rows.
+bool tile_ok(const SolveDims &d, bool big, int v, int lr, int bt)
+{
+    const int vm = 16 / (int)prec_bytes(d.prec);
+    if ((v != 1 && v != 2 && v != 4 && v != 8) || v > vm) return false;
+    if (bt != 128 && bt != 256) return false;
+    if (lr == 32) return d.Ap % (32 * v) == 0;
+    if (lr != 16 && lr != 8 && lr != 4) return false;
+    return !big && (v == vm || v == vm / 2) && v * lr == d.Ap;
+}
+
+int default_v(const SolveDims &d)
+{
+    int v = 16 / (int)prec_bytes(d.prec);
+    while (v > 1 && d.Ap % (32 * v)) v >>= 1;
+    return v;
+}
+
+// The tile of a streaming solve.  Fields the caller set are kept; the rest
+// come from the problem's cache or from timing every candidate tile over a
+// few plain steps on the live state (*timed then asks the caller to set the
+// initial state again).  Every tile computes the same results.
+int pick_tile(sbx_ctx *ctx, std::map<std::string, Tile> &cache, SolveDims &d, const DevCsr &J,
+              const sbx_params *pr, bool *timed)
+{
+    *timed = false;
+    const bool big = J.unit && J.nchunks > 0;
+    const int fv = pr->lane_agents, flr = pr->row_lanes, fbt = pr->block_threads;
+    std::vector<Tile> cands;
+    const int vs[4] = {8, 4, 2, 1}, lrs[4] = {32, 16, 8, 4}, bts[2] = {256, 128};
+    for (int v : vs)
+        for (int lr : lrs)
+            for (int bt : bts) {
+                if ((fv && v != fv) || (flr && lr != flr) || (fbt && bt != fbt)) continue;
+                if (tile_ok(d, big, v, lr, bt)) cands.push_back(Tile{v, lr, bt});
+            }
+    if (cands.empty())
+        return fail(ctx, SBX_ERR_ARG, "no streaming tile fits lane_agents / row_lanes / block_threads");
+    auto apply = [&](const Tile &t) {
+        d.tv = t.v;
+        d.tlr = t.lr;
+        d.tbt = t.bt;
+    };
+    apply(cands[0]);
+    if (cands.size() == 1) return SBX_OK;
+    if (pr->flags & SBX_FLAG_NO_TUNE) {
+        // fixed heuristic: widest dividing vector, whole-warp rows, 256 threads
+        for (const Tile &t : cands)
+            if (t.v == default_v(d) && t.lr == 32 && t.bt == 256) apply(t);
+        return SBX_OK;
+    }
+    char key[96];
+    snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d", d.prec, d.Ap, d.fused, fv, flr, fbt);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+        apply(it->second);
+        return SBX_OK;
+    }
+    cudaStream_t s = ctx->stream;
+    Work &w = ctx->w;
+    // about 2 ms of launches per measurement, best of two rounds
+    CK(launch_plain_steps(d, J, w, 1, s));
+    CK(cudaEventRecord(ctx->ev0, s));
+    CK(launch_plain_steps(d, J, w, 1, s));
+    CK(cudaEventRecord(ctx->ev1, s));
+    CK(cudaEventSynchronize(ctx->ev1));
+    float one = 0;
+    CK(cudaEventElapsedTime(&one, ctx->ev0, ctx->ev1));
+    const int reps = std::max(3, std::min(64, (int)(2.0 / std::max(one, 1e-3f))));
+    std::vector<float> best(cands.size(), 1e30f);
+    for (int round = 0; round < 2; round++)
+        for (size_t i = 0; i < cands.size(); i++) {
+            apply(cands[i]);
+            CK(launch_plain_steps(d, J, w, 1, s));
+            CK(cudaEventRecord(ctx->ev0, s));
+            CK(launch_plain_steps(d, J, w, reps, s));
+            CK(cudaEventRecord(ctx->ev1, s));
+            CK(cudaEventSynchronize(ctx->ev1));
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+            best[i] = std::min(best[i], ms / reps);
+        }
+    size_t bi = 0;
+    for (size_t i = 1; i < cands.size(); i++)
+        if (best[i] < best[bi]) bi = i;
+    apply(cands[bi]);
+    cache[key] = cands[bi];
+    *timed = true;
+    return SBX_OK;
+}
+
+// Trace of the last solve: records to the context; the first window whose
+// best cut reaches target gives the time and steps to target.
+int read_trace(sbx_ctx *ctx, const SolveDims &d, int32_t traced, double target, sbx_result *res)
+{
+    res->time_to_target_us = -1;
+    res->steps_to_target = -1;
+    ctx->trace.clear();
+    if (!d.trace) return SBX_OK;
+    const size_t cnt = std::min((size_t)std::max(traced, 0), ctx->w.cap_trace);
+    ctx->trace.resize(cnt);
+    if (cnt)
+        CK(cudaMemcpy(ctx->trace.data(), ctx->w.trace, sizeof(TraceRec) * cnt, cudaMemcpyDeviceToHost));
+    if (target > 0)
+        for (const TraceRec &r : ctx->trace)
+            if (r.best >= target) {
+                res->time_to_target_us = (double)r.t_ns / 1000.0;
+                res->steps_to_target = r.steps;
+                break;
+            }
+    return SBX_OK;
+}
+
 // The streaming loop of one solve: the pre-step Update_XY, then windows of
 // d.period steps (a captured CUDA graph per window, replayed), with the
 // all-bifurcated exit polled when d.uw.  Profile mode launches directly and
@@ -386,14 +517,19 @@ int run_stream(sbx_ctx *ctx, const void *key_obj, const SolveDims &d, const DevC
     cudaStream_t s = ctx->stream;
     int launches = 0;
     double kernel_ms = 0;
+    if (d.trace) {
+        CK(launch_trace_start(ctx->w, s));
+        launches++;
+    }
     CK(launch_prestep(d, J, ctx->w, s, &launches));
     if (nchunks) {
         int per_chunk = 0;
         if (use_graph) {
             char key[256];
-            snprintf(key, sizeof key, "%p/%lld/%d/%d/%d/%d/%d/%d/%d/%d/%.17g/%llu/%p", key_obj,
-                     (long long)d.n, d.A, d.prec, d.period, d.fused, d.uw, d.threshold, (int)d.pdl,
-                     d.steps, d.c0, (unsigned long long)g_alloc_gen, (void *)s);
+            snprintf(key, sizeof key, "%p/%lld/%d/%d/%d/%d/%d/%d/%d/%d/%.17g/%llu/%p/%d/%d/%d/%d",
+                     key_obj, (long long)d.n, d.A, d.prec, d.period, d.fused, d.uw, d.threshold,
+                     (int)d.pdl, d.steps, d.c0, (unsigned long long)g_alloc_gen, (void *)s, d.tv,
+                     d.tlr, d.tbt, d.trace);
             if (!ctx->gexec || ctx->gkey != key) {
                 if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
                 ctx->gexec = nullptr;
@@ -462,6 +598,7 @@ int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_r
     d.xi0 = xi0_of(p->J);
     d.c0 = d.dt * d.xi0;
     d.pdl = !(pr->flags & SBX_FLAG_NO_PDL);
+    d.trace = (pr->trace || pr->target > 0) ? 1 : 0;
     const bool profile = (pr->flags & SBX_FLAG_PROFILE) != 0;
     const bool use_graph = !(pr->flags & SBX_FLAG_NO_GRAPH) && !profile;
     double kernel_ms = 0;
@@ -469,15 +606,22 @@ int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_r
     const int64_t nchunks = run > 0 ? (run + d.period - 1) / d.period : 0;
     const int64_t total = nchunks * d.period;
     cudaStream_t s = ctx->stream;
+    if (d.trace && pr->kernel == SBX_KERNEL_RESIDENT)
+        return fail(ctx, SBX_ERR_UNSUPPORTED, "trace / target: streaming kernel only");
     int rc = ensure_common(ctx, d, total, p->J.nchunks);
     if (rc) return rc;
     if ((rc = upload_coef(ctx, d, total))) return rc;
     if ((rc = init_state(ctx, d, pr->seed, false))) return rc;
 
     int ka = 0;
-    if (pr->kernel != SBX_KERNEL_STREAM) ka = resident_pick_ka(d, p->J, pr->agents_per_block);
+    if (pr->kernel != SBX_KERNEL_STREAM && !d.trace) ka = resident_pick_ka(d, p->J, pr->agents_per_block);
     if (pr->kernel == SBX_KERNEL_RESIDENT && !ka)
         return fail(ctx, SBX_ERR_UNSUPPORTED, "resident kernel: shape does not fit on chip (or FP64)");
+    if (!ka) {
+        bool timed = false;
+        if ((rc = pick_tile(ctx, p->tiles, d, p->J, pr, &timed))) return rc;
+        if (timed && (rc = init_state(ctx, d, pr->seed, false))) return rc;
+    }
     int launches = 0, hot = 0;
     CK(cudaEventRecord(ctx->ev0, s));
     if (ka) {
@@ -520,6 +664,12 @@ int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_r
     for (uint8_t b : bif) res->bifurcated += b;
     res->kernel_used = ka ? SBX_KERNEL_RESIDENT : SBX_KERNEL_STREAM;
     res->agents_per_block = ka;
+    if (!ka) {
+        res->lane_agents = d.tv ? d.tv : default_v(d);
+        res->row_lanes = d.tlr;
+        res->block_threads = d.tbt;
+    }
+    if ((rc = read_trace(ctx, d, ctl[CTL_TRACED], pr->target, res))) return rc;
     if (ka) {
         res->kernel_launches = hot;
         res->kernel_ms = profile ? ms : 0;
@@ -620,6 +770,8 @@ int solve_tsp(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
     CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     // Decode and statistics, src/ising_tsp.cu:188-239 and :272-287.
     memset(res, 0, sizeof *res);
+    res->time_to_target_us = -1;
+    res->steps_to_target = -1;
     std::vector<double> all;
     double total_len = 0, mn = DBL_MAX, mx = -DBL_MAX;
     int32_t best = -1;
@@ -750,6 +902,8 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
     if (count < 1 || !problems || !agents || !pr || !res) return fail(ctx, SBX_ERR_ARG, "null argument");
     if (pr->update_window)
         return fail(ctx, SBX_ERR_UNSUPPORTED, "batched solve: update_window (per-instance exit) is not supported");
+    if (pr->trace || pr->target > 0)
+        return fail(ctx, SBX_ERR_UNSUPPORTED, "batched solve: trace / target are not supported");
     if (pr->steps < 0 || pr->precision < 0 || pr->precision > 3 || pr->run_steps < 0 || pr->period < 0)
         return fail(ctx, SBX_ERR_ARG, "bad params");
     std::string key;
@@ -822,6 +976,11 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
             rand_seed_window(pr->seed + (uint32_t)c.idx[i], inst[i].V0);
         }
         if ((rc = init_instances(ctx, d, inst, false))) return rc;
+        if (nchunks) {
+            bool timed = false;
+            if ((rc = pick_tile(ctx, c.tiles, d, c.J, pr, &timed))) return rc;
+            if (timed && (rc = init_instances(ctx, d, inst, false))) return rc;
+        }
         int launches = 0;
         double kms = 0;
         CK(cudaEventRecord(ctx->ev0, s));
@@ -847,6 +1006,11 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
             }
             sbx_result *r = &res[gi];
             memset(r, 0, sizeof *r);
+            r->time_to_target_us = -1;
+            r->steps_to_target = -1;
+            r->lane_agents = d.tv ? d.tv : default_v(d);
+            r->row_lanes = d.tlr;
+            r->block_threads = d.tbt;
             stats(cut, r);
             r->time_us = ms * 1000.0;
             r->xi0 = c.xi0[i];
@@ -969,7 +1133,7 @@ int sbx_destroy(sbx_ctx *ctx)
     Work &w = ctx->w;
     void *ptrs[] = {w.x, w.y, w.x2, w.S[0], w.S[1], w.Wp, w.fin, w.chg, w.newmask, w.stab, w.bif,
                     w.prev, w.ctl, w.wincount, w.visits, w.ab, w.sched, w.eacc, w.cut, w.trace,
-                    w.tours, w.valid, w.rjump, w.coef32, w.coef64, w.part, w.rinst};
+                    w.tours, w.valid, w.rjump, w.coef32, w.coef64, w.part, w.rinst, w.trace_t0};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
@@ -1148,7 +1312,8 @@ int sbx_solve(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
     if (!ctx || !p || !pr || !res) return fail(ctx, SBX_ERR_ARG, "null argument");
     if (p->ctx != ctx) return fail(ctx, SBX_ERR_ARG, "problem belongs to another (or a destroyed) context");
     if (pr->agents < 1 || pr->steps < 0 || !(pr->dt == pr->dt) || pr->precision < 0 ||
-        pr->precision > 3 || pr->run_steps < 0 || pr->period < 0 || pr->threshold < 0)
+        pr->precision > 3 || pr->run_steps < 0 || pr->period < 0 || pr->threshold < 0 ||
+        pr->lane_agents < 0 || pr->row_lanes < 0 || pr->block_threads < 0 || !(pr->target == pr->target))
         return fail(ctx, SBX_ERR_ARG, "bad params (agents >= 1, steps >= 0, precision 0..3)");
     if (pr->agents < 2 && !p->tsp) {
         // the reference's std dev divides by agents-1; one agent is allowed
@@ -1158,6 +1323,7 @@ int sbx_solve(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
         return fail(ctx, SBX_ERR_NOMEM, "state larger than the device");
     CK(cudaSetDevice(ctx->device));
     ctx->have = false;
+    if (p->tsp && pr->target > 0) return fail(ctx, SBX_ERR_UNSUPPORTED, "target: MaxCut only");
     return p->tsp ? solve_tsp(ctx, p, pr, res, agent_values) : solve_maxcut(ctx, p, pr, res, agent_values);
 }
 
@@ -1224,14 +1390,21 @@ int sbx_solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, c
     return solve_batch(ctx, count, problems, agents, params, res, agent_values, batch_time_us);
 }
 
-int sbx_get_trace(sbx_ctx *ctx, int64_t cap, int64_t *steps, double *best, int64_t *count)
+int sbx_get_trace(sbx_ctx *ctx, int64_t cap, int64_t *steps, double *best, double *t_us, int64_t *count)
 {
-    (void)cap;
-    (void)steps;
-    (void)best;
     if (!ctx) return SBX_ERR_ARG;
     if (count) *count = 0;
-    return fail(ctx, SBX_ERR_UNSUPPORTED, "trace not recorded");
+    if (!ctx->have || ctx->last_tsp || ctx->trace.empty())
+        return fail(ctx, SBX_ERR_STATE, "no traced MaxCut solve (params.trace or params.target)");
+    const int64_t k = std::min<int64_t>(std::max<int64_t>(cap, 0), (int64_t)ctx->trace.size());
+    for (int64_t i = 0; i < k; i++) {
+        const TraceRec &r = ctx->trace[(size_t)i];
+        if (steps) steps[i] = r.steps;
+        if (best) best[i] = r.best;
+        if (t_us) t_us[i] = (double)r.t_ns / 1000.0;
+    }
+    if (count) *count = (int64_t)ctx->trace.size();
+    return SBX_OK;
 }
 
 }  // extern "C"

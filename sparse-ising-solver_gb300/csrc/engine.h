@@ -56,7 +56,16 @@ struct DevCsr {
 };
 
 // Control words shared by the kernels of one solve.
-enum Ctl { CTL_STEP = 0, CTL_STOP = 1, CTL_WINDOWS = 2, CTL_NBIF = 3, CTL_N = 8 };
+enum Ctl { CTL_STEP = 0, CTL_STOP = 1, CTL_WINDOWS = 2, CTL_NBIF = 3, CTL_TRACED = 4, CTL_N = 8 };
+
+// One window of a traced solve: SB steps run, best cut over the agents of
+// the window spins, nanoseconds since the loop began (device clock).
+struct TraceRec {
+    long long steps;
+    double best;
+    long long t_ns;
+    long long pad;
+};
 
 // Device buffers of one solve (grown on demand, owned by the context).
 struct Work {
@@ -73,7 +82,8 @@ struct Work {
     uint32_t *part = nullptr;             // heavy-row partial counts
     unsigned long long *eacc = nullptr;   // per-agent cut accumulators
     double *cut = nullptr;                // per-agent cuts
-    double *trace = nullptr;              // per-window best cut
+    TraceRec *trace = nullptr;            // per-window records; trace_t0: loop start
+    long long *trace_t0 = nullptr;
     int32_t *tours = nullptr, *valid = nullptr;
     uint32_t *rjump = nullptr;            // rand jump matrices (computed once)
     RandInst *rinst = nullptr;            // init instances of the current solve
@@ -82,7 +92,7 @@ struct Work {
     size_t cap_x = 0, cap_y = 0, cap_x2 = 0, cap_S0 = 0, cap_S1 = 0, cap_Wp = 0, cap_fin = 0,
            cap_chg = 0, cap_new = 0, cap_stab = 0, cap_bif = 0, cap_prev = 0, cap_ctl = 0,
            cap_win = 0, cap_visits = 0, cap_ab = 0, cap_sched = 0, cap_eacc = 0, cap_cut = 0,
-           cap_trace = 0, cap_tours = 0, cap_valid = 0, cap_rj = 0, cap_c32 = 0, cap_c64 = 0, cap_part = 0, cap_rinst = 0;
+           cap_trace = 0, cap_t0 = 0, cap_tours = 0, cap_valid = 0, cap_rj = 0, cap_c32 = 0, cap_c64 = 0, cap_part = 0, cap_rinst = 0;
     bool rjump_ready = false;
 };
 
@@ -96,6 +106,10 @@ struct SolveDims {
     int fused = 1, uw = 0;
     double dt = 0.1, xi0 = 0, c0 = 0;
     bool pdl = true;
+    // streaming step tile: agents per lane (0: widest vector that divides
+    // Ap), lanes per row (32, 16, 8, 4), threads per CTA
+    int32_t tv = 0, tlr = 32, tbt = 256;
+    int trace = 0;           // per-window best-cut records (streaming MaxCut)
 };
 
 // ---- launchers (k_*.cu) ----
@@ -117,6 +131,11 @@ cudaError_t launch_chunk(const SolveDims &d, const DevCsr &J, Work &w, cudaStrea
                          int *launches, cudaEvent_t *evs = nullptr);
 cudaError_t launch_cut(const SolveDims &d, const DevCsr &J, Work &w, const uint32_t *plane,
                        cudaStream_t s, int *launches);
+// count plain (non-window) steps of the solve's kind at step 0: the
+// autotuner's timing runs.
+cudaError_t launch_plain_steps(const SolveDims &d, const DevCsr &J, Work &w, int count, cudaStream_t s);
+// Traced solves: stamp the loop start on the device clock.
+cudaError_t launch_trace_start(Work &w, cudaStream_t s);
 // Integer weights, block-diagonal J: eacc[instance][Ap] += s_r sum_j J_rj s_j.
 cudaError_t launch_cut_batch(const SolveDims &d, const DevCsr &J, const uint32_t *plane,
                              unsigned long long *eacc, cudaStream_t s);

@@ -14,10 +14,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libsbx.so")
 
 OK = 0
+ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_IO, ERR_FORMAT, ERR_UNSUPPORTED, ERR_NODEVICE, ERR_STATE = \
+    -1, -2, -3, -4, -5, -6, -7, -8
 F32, BF16, F16, F64 = 0, 1, 2, 3
 KERNEL_AUTO, KERNEL_STREAM, KERNEL_RESIDENT = 0, 1, 2
 DIST_EUC_2D, DIST_GEO, DIST_EUC_2D_FLOAT = 0, 1, 2
-FLAG_NO_PDL, FLAG_NO_GRAPH, FLAG_PROFILE = 1, 2, 4
+FLAG_NO_PDL, FLAG_NO_GRAPH, FLAG_PROFILE, FLAG_NO_TUNE = 1, 2, 4, 8
 PRECISIONS = {"f32": F32, "bf16": BF16, "f16": F16, "f64": F64}
 NOALLOC_MAX_WORDS = 1 << 21   # SBX_NOALLOC_MAX_WORDS in include/sbx.h
 
@@ -37,7 +39,8 @@ class Params(C.Structure):
                 ("fused", C.c_int32), ("update_window", C.c_int32), ("period", C.c_int32),
                 ("threshold", C.c_int32), ("precision", C.c_int32), ("seed", C.c_uint32),
                 ("kernel", C.c_int32), ("agents_per_block", C.c_int32), ("trace", C.c_int32),
-                ("flags", C.c_uint32), ("run_steps", C.c_int32)]
+                ("flags", C.c_uint32), ("run_steps", C.c_int32), ("lane_agents", C.c_int32),
+                ("row_lanes", C.c_int32), ("block_threads", C.c_int32), ("target", C.c_double)]
 
 
 class Result(C.Structure):
@@ -46,8 +49,10 @@ class Result(C.Structure):
                 ("xi0", C.c_double), ("steps_run", C.c_int64), ("windows_run", C.c_int64),
                 ("bifurcated", C.c_int64), ("valid", C.c_int64), ("best_agent", C.c_int32),
                 ("kernel_used", C.c_int32), ("agents_per_block", C.c_int32),
-                ("reserved", C.c_int32), ("kernel_ms", C.c_double),
-                ("kernel_launches", C.c_int64), ("gpu_launches", C.c_int64)]
+                ("lane_agents", C.c_int32), ("row_lanes", C.c_int32), ("block_threads", C.c_int32),
+                ("kernel_ms", C.c_double), ("kernel_launches", C.c_int64),
+                ("gpu_launches", C.c_int64), ("time_to_target_us", C.c_double),
+                ("steps_to_target", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -258,6 +263,17 @@ class Context:
         s = np.empty(n * agents, np.int32)
         _check("sbx_get_state", lib().sbx_get_state(self._c, _p(x), _p(y), _p(s)))
         return x, y, s
+
+    def trace(self, cap=1 << 16):
+        """Per-window (steps, best cut, microseconds) of the last traced solve."""
+        st = np.empty(cap, np.int64)
+        b = np.empty(cap)
+        t = np.empty(cap)
+        cnt = C.c_int64()
+        _check("sbx_get_trace", lib().sbx_get_trace(self._c, C.c_int64(cap), _p(st), _p(b), _p(t),
+                                                    C.byref(cnt)))
+        k = min(cnt.value, cap)
+        return st[:k].copy(), b[:k].copy(), t[:k].copy()
 
     def tours(self, N, agents):
         t = np.empty(N * agents, np.int32)

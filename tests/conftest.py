@@ -21,3 +21,22 @@ def oracle():
     import sbo
     sbo.lib()
     return sbo
+
+
+def oracle_graph(oracle, g):
+    """The oracle's CSR of an sbx.Graph."""
+    return oracle.Graph(g.n, g.rowptr, g.col, g.val, g.wsum)
+
+
+def oracle_first_steps(oracle, og, A, seed, dt, max_steps, k, fused):
+    """The oracle's state after the pre-step and the first k steps of a
+    max_steps schedule (src/ising.cu:188 then k kernel launches)."""
+    x, y = oracle.init_maxcut(og.n, A, seed)
+    oracle.update_xy(x, y, 0, max_steps, dt)
+    x0 = oracle.xi0(og)
+    for step in range(k):
+        if fused:
+            oracle.fused_step(og, x, y, A, step, max_steps, dt, x0)
+        else:
+            oracle.unfused_step(og, x, y, A, step, max_steps, dt, x0)
+    return x, y

@@ -13,7 +13,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN
+from conftest import GOLDEN, oracle_first_steps, oracle_graph
 
 import sbx
 
@@ -63,22 +63,8 @@ def test_fp64_maxcut_bitexact_with_reference_fixture(ctx, name):
     assert r["xi0"] == float(ref["xi0"])
 
 
-def _oracle_graph(oracle, g):
-    return oracle.Graph(g.n, g.rowptr, g.col, g.val, g.wsum)
-
-
-def _oracle_first_steps(oracle, og, A, seed, dt, max_steps, k, fused):
-    """The oracle's state after the pre-step and the first k steps of a
-    max_steps schedule (src/ising.cu:188 then k kernel launches)."""
-    x, y = oracle.init_maxcut(og.n, A, seed)
-    oracle.update_xy(x, y, 0, max_steps, dt)
-    x0 = oracle.xi0(og)
-    for step in range(k):
-        if fused:
-            oracle.fused_step(og, x, y, A, step, max_steps, dt, x0)
-        else:
-            oracle.unfused_step(og, x, y, A, step, max_steps, dt, x0)
-    return x, y
+_oracle_graph = oracle_graph
+_oracle_first_steps = oracle_first_steps
 
 
 @pytest.mark.parametrize("kernel", [sbx.KERNEL_STREAM, sbx.KERNEL_RESIDENT])

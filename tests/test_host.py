@@ -2,6 +2,7 @@
 every declared entry point, the loaders reproduce the reference's CSR / TSPLIB
 parse (fixtures from the reference's own csr.cpp / tsp_cpu.cpp), errors come
 back as status codes, and the generators are seeded and well formed."""
+import ctypes as C
 import os
 import re
 import subprocess
@@ -26,6 +27,27 @@ def test_library_exports_every_declared_symbol():
     lib = sbx.lib()
     for name in declared:
         assert hasattr(lib, name)
+
+
+def test_struct_layout_matches_header(tmp_path):
+    """The ctypes mirror of sbx_params / sbx_result has the C layout: every
+    field at the offset gcc gives it, and the same total size."""
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "sbx.h"', 'int main(void) {']
+    for cname, py in (("sbx_params", sbx.Params), ("sbx_result", sbx.Result)):
+        lines.append('printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in py._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines += ['return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(l.rsplit(" ", 1) for l in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                          check=True).stdout.splitlines())
+    for cname, py in (("sbx_params", sbx.Params), ("sbx_result", sbx.Result)):
+        assert int(got[cname + " size"]) == C.sizeof(py)
+        for f, _ in py._fields_:
+            assert int(got["%s %s" % (cname, f)]) == getattr(py, f).offset, (cname, f)
 
 
 def test_version_and_strerror():
