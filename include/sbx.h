@@ -77,6 +77,9 @@ typedef struct sbx_params {
     int32_t row_lanes;      /* lanes per row: 32, or 16/8/4 (several rows per
                                warp; then lane_agents * row_lanes = padded agents) */
     int32_t block_threads;  /* threads per CTA: 128 or 256 */
+    int32_t count_mode;     /* +-1 weights: 1 byte counters per lane, 2 bit
+                               planes per sign word (neighbours split across
+                               the word's lanes); 0: autotuned */
     double target;          /* MaxCut: a cut; > 0 records the per-window best
                                cut (as trace = 1) and times its first reach */
 } sbx_params;
@@ -96,6 +99,7 @@ typedef struct sbx_result {
     int32_t lane_agents;    /* streaming tile used (0 for other kernels) */
     int32_t row_lanes;
     int32_t block_threads;
+    int32_t count_mode;
     double kernel_ms;       /* SBX_FLAG_PROFILE: summed hot-kernel time */
     int64_t kernel_launches;/* hot-kernel launches issued by the solve */
     int64_t gpu_launches;   /* all kernel launches issued by the solve */
@@ -152,10 +156,14 @@ int sbx_get_trace(sbx_ctx *ctx, int64_t cap, int64_t *steps, double *best,
 /* ---- batched MaxCut: many independent instances, one launch per step ---- */
 /* Each instance keeps its own xi0, weight sum and agent count; all share
  * dt/steps/precision from params.  Per-instance results go to res[count]
- * and agent_values (concatenated, sum of agents) when given. */
+ * and agent_values (concatenated, sum of agents) when given.  targets
+ * (optional, [count]): per-instance cuts; each instance's first window whose
+ * best cut reaches its target sets its time_to_target_us (from the start of
+ * the run of its agent class) and steps_to_target. */
 int sbx_solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems,
                     const int32_t *agents, const sbx_params *params,
-                    sbx_result *res, double *agent_values, double *batch_time_us);
+                    const double *targets, sbx_result *res, double *agent_values,
+                    double *batch_time_us);
 
 /* ---- fused steps without device allocation ---- */
 /* No counterpart in the reference.  For callers that cannot allocate device

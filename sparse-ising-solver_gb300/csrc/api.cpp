@@ -28,7 +28,7 @@ using namespace sbx;
 
 // Streaming step tile (agents per lane, lanes per row, threads per CTA).
 struct Tile {
-    int32_t v = 0, lr = 32, bt = 256;
+    int32_t v = 0, lr = 32, bt = 256, cm = 0;
 };
 
 struct sbx_problem {
@@ -134,11 +134,17 @@ void free_csr(DevCsr &J)
     cudaFree(J.c0r32);
     cudaFree(J.c0r64);
     cudaFree(J.rinst);
+    cudaFree(J.iagents);
+    cudaFree(J.iwsum);
+    J.iagents = nullptr;
+    J.iwsum = nullptr;
+    J.ninst = 0;
     J.c0r32 = nullptr;
     J.c0r64 = nullptr;
     J.rinst = nullptr;
     J.hchunk = J.chunk_row = nullptr;
     J.nchunks = 0;
+    J.nheavy = 0;
     J.rowptr = nullptr;
     J.colw = nullptr;
     J.vald = nullptr;
@@ -216,6 +222,7 @@ int upload_csr(sbx_ctx *ctx, DevCsr &J, int64_t n, int64_t nnz, const int32_t *r
             for (int32_t c = 0; c < (deg + kHeavy - 1) / kHeavy; c++) crow.push_back((int32_t)r);
         }
         J.nchunks = (int32_t)crow.size();
+        for (int64_t r = 0; r < n; r++) J.nheavy += hchunk[r] >= 0;
         CK(cudaMalloc(&J.hchunk, sizeof(int32_t) * n));
         CK(cudaMalloc(&J.chunk_row, sizeof(int32_t) * crow.size()));
         CK(cudaMemcpy(J.hchunk, hchunk.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
@@ -287,7 +294,10 @@ int ensure_common(sbx_ctx *ctx, const SolveDims &d, int64_t total_steps, int32_t
     CK(grow(w.prev, w.cap_prev, (size_t)d.Ap));
     CK(grow(w.ctl, w.cap_ctl, (size_t)CTL_N));
     CK(grow(w.eacc, w.cap_eacc, (size_t)d.Ap));
-    if (J_nchunks) CK(grow(w.part, w.cap_part, (size_t)J_nchunks * d.Ap * 2));
+    if (J_nchunks) {
+        CK(grow(w.part, w.cap_part, (size_t)J_nchunks * d.Ap * 2));
+        CK(grow(w.hcount, w.cap_hcount, (size_t)J_nchunks * d.W));
+    }
     CK(grow(w.cut, w.cap_cut, (size_t)d.Ap));
     const int64_t nwin = d.period > 0 ? total_steps / d.period + 2 : 2;
     CK(grow(w.wincount, w.cap_win, (size_t)nwin));
@@ -309,6 +319,7 @@ int ensure_common(sbx_ctx *ctx, const SolveDims &d, int64_t total_steps, int32_t
     CK(cudaMemsetAsync(w.prev, 0, (size_t)d.Ap, s));
     CK(cudaMemsetAsync(w.ctl, 0, CTL_N * 4, s));
     CK(cudaMemsetAsync(w.wincount, 0, (size_t)nwin * 4, s));
+    if (J_nchunks) CK(cudaMemsetAsync(w.hcount, 0, (size_t)J_nchunks * d.W * 4, s));
     return SBX_OK;
 }
 
@@ -422,31 +433,36 @@ int pick_tile(sbx_ctx *ctx, std::map<std::string, Tile> &cache, SolveDims &d, co
     *timed = false;
     const bool big = J.unit && J.nchunks > 0;
     const int fv = pr->lane_agents, flr = pr->row_lanes, fbt = pr->block_threads;
+    const int fcm = pr->count_mode;   // 1 byte counters, 2 bit planes
     std::vector<Tile> cands;
     const int vs[4] = {8, 4, 2, 1}, lrs[4] = {32, 16, 8, 4}, bts[2] = {256, 128};
-    for (int v : vs)
-        for (int lr : lrs)
-            for (int bt : bts) {
-                if ((fv && v != fv) || (flr && lr != flr) || (fbt && bt != fbt)) continue;
-                if (tile_ok(d, big, v, lr, bt)) cands.push_back(Tile{v, lr, bt});
-            }
+    for (int cm = 0; cm < (J.unit ? 2 : 1); cm++)
+        for (int v : vs)
+            for (int lr : lrs)
+                for (int bt : bts) {
+                    if ((fv && v != fv) || (flr && lr != flr) || (fbt && bt != fbt) || (fcm && cm != fcm - 1))
+                        continue;
+                    if (tile_ok(d, big, v, lr, bt)) cands.push_back(Tile{v, lr, bt, cm});
+                }
     if (cands.empty())
         return fail(ctx, SBX_ERR_ARG, "no streaming tile fits lane_agents / row_lanes / block_threads");
     auto apply = [&](const Tile &t) {
         d.tv = t.v;
         d.tlr = t.lr;
         d.tbt = t.bt;
+        d.tcm = t.cm;
     };
     apply(cands[0]);
     if (cands.size() == 1) return SBX_OK;
     if (pr->flags & SBX_FLAG_NO_TUNE) {
-        // fixed heuristic: widest dividing vector, whole-warp rows, 256 threads
+        // fixed heuristic: widest dividing vector, whole-warp rows, 256
+        // threads, byte counters
         for (const Tile &t : cands)
-            if (t.v == default_v(d) && t.lr == 32 && t.bt == 256) apply(t);
+            if (t.v == default_v(d) && t.lr == 32 && t.bt == 256 && t.cm == 0) apply(t);
         return SBX_OK;
     }
     char key[96];
-    snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d", d.prec, d.Ap, d.fused, fv, flr, fbt);
+    snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d/%d", d.prec, d.Ap, d.fused, fv, flr, fbt, fcm);
     auto it = cache.find(key);
     if (it != cache.end()) {
         apply(it->second);
@@ -526,10 +542,10 @@ int run_stream(sbx_ctx *ctx, const void *key_obj, const SolveDims &d, const DevC
         int per_chunk = 0;
         if (use_graph) {
             char key[256];
-            snprintf(key, sizeof key, "%p/%lld/%d/%d/%d/%d/%d/%d/%d/%d/%.17g/%llu/%p/%d/%d/%d/%d",
+            snprintf(key, sizeof key, "%p/%lld/%d/%d/%d/%d/%d/%d/%d/%d/%.17g/%llu/%p/%d/%d/%d/%d/%d",
                      key_obj, (long long)d.n, d.A, d.prec, d.period, d.fused, d.uw, d.threshold,
                      (int)d.pdl, d.steps, d.c0, (unsigned long long)g_alloc_gen, (void *)s, d.tv,
-                     d.tlr, d.tbt, d.trace);
+                     d.tlr, d.tbt, d.tcm, d.trace);
             if (!ctx->gexec || ctx->gkey != key) {
                 if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
                 ctx->gexec = nullptr;
@@ -668,6 +684,7 @@ int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_r
         res->lane_agents = d.tv ? d.tv : default_v(d);
         res->row_lanes = d.tlr;
         res->block_threads = d.tbt;
+        res->count_mode = d.tcm + 1;
     }
     if ((rc = read_trace(ctx, d, ctl[CTL_TRACED], pr->target, res))) return rc;
     if (ka) {
@@ -858,6 +875,11 @@ int build_class(sbx_ctx *ctx, BatchClass &c)
     CK(cudaMalloc(&c.J.c0r32, sizeof(float) * n));
     CK(cudaMalloc(&c.J.c0r64, sizeof(double) * n));
     CK(cudaMemcpy(c.J.rinst, rinst.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+    c.J.ninst = (int32_t)c.probs.size();
+    CK(cudaMalloc(&c.J.iagents, sizeof(int32_t) * c.J.ninst));
+    CK(cudaMalloc(&c.J.iwsum, sizeof(double) * c.J.ninst));
+    CK(cudaMemcpy(c.J.iagents, c.agents.data(), sizeof(int32_t) * c.J.ninst, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c.J.iwsum, c.wsum.data(), sizeof(double) * c.J.ninst, cudaMemcpyHostToDevice));
     return SBX_OK;
 }
 
@@ -897,13 +919,14 @@ void free_batch(sbx_ctx *ctx)
 // position), the shared step kernels (the grid-stride row scheduler balances
 // instances of any size), and per-instance exact cuts and statistics.
 int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const int32_t *agents,
-                const sbx_params *pr, sbx_result *res, double *agent_values, double *batch_time_us)
+                const sbx_params *pr, const double *targets, sbx_result *res, double *agent_values,
+                double *batch_time_us)
 {
     if (count < 1 || !problems || !agents || !pr || !res) return fail(ctx, SBX_ERR_ARG, "null argument");
     if (pr->update_window)
         return fail(ctx, SBX_ERR_UNSUPPORTED, "batched solve: update_window (per-instance exit) is not supported");
-    if (pr->trace || pr->target > 0)
-        return fail(ctx, SBX_ERR_UNSUPPORTED, "batched solve: trace / target are not supported");
+    if (pr->target > 0)
+        return fail(ctx, SBX_ERR_ARG, "batched solve: per-instance targets go in the targets array");
     if (pr->steps < 0 || pr->precision < 0 || pr->precision > 3 || pr->run_steps < 0 || pr->period < 0)
         return fail(ctx, SBX_ERR_ARG, "bad params");
     std::string key;
@@ -963,10 +986,14 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
         d.uw = 0;
         d.dt = pr->dt;
         d.pdl = !(pr->flags & SBX_FLAG_NO_PDL);
+        d.trace = (pr->trace || targets) ? 2 : 0;
         const int32_t run = pr->run_steps > 0 ? std::min(pr->run_steps, pr->steps) : pr->steps;
         const int64_t nchunks = run > 0 ? (run + d.period - 1) / d.period : 0;
         const int64_t total = nchunks * d.period;
         if ((rc = ensure_common(ctx, d, total, c.J.nchunks))) return rc;
+        const size_t ne = c.probs.size() * (size_t)c.Ap;
+        CK(grow(ctx->w.eacc, ctx->w.cap_eacc, ne));
+        if (d.trace) CK(grow(ctx->w.btrace, ctx->w.cap_btrace, ctx->w.cap_trace * c.probs.size()));
         if ((rc = upload_coef(ctx, d, total))) return rc;
         std::vector<RandInst> inst(c.probs.size());
         for (size_t i = 0; i < c.probs.size(); i++) {
@@ -986,8 +1013,18 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
         CK(cudaEventRecord(ctx->ev0, s));
         if ((rc = run_stream(ctx, &c.J, d, c.J, nchunks, profile, use_graph, &launches, &kms))) return rc;
         CK(cudaEventRecord(ctx->ev1, s));
-        const size_t ne = c.probs.size() * (size_t)c.Ap;
-        CK(grow(ctx->w.eacc, ctx->w.cap_eacc, ne));
+        // per-instance best cut of every window: the first reaching the target
+        std::vector<double> bt;
+        std::vector<TraceRec> recs;
+        if (d.trace) {
+            const size_t nw = std::min((size_t)nchunks, ctx->w.cap_trace);
+            bt.resize(nw * c.probs.size());
+            recs.resize(nw);
+            if (nw) {
+                CK(cudaMemcpyAsync(bt.data(), ctx->w.btrace, sizeof(double) * bt.size(), cudaMemcpyDeviceToHost, s));
+                CK(cudaMemcpyAsync(recs.data(), ctx->w.trace, sizeof(TraceRec) * nw, cudaMemcpyDeviceToHost, s));
+            }
+        }
         CK(cudaMemsetAsync(ctx->w.eacc, 0, sizeof(unsigned long long) * ne, s));
         CK(launch_cut_batch(d, c.J, ctx->w.Wp, ctx->w.eacc, s));
         std::vector<long long> E(ne);
@@ -1011,6 +1048,14 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
             r->lane_agents = d.tv ? d.tv : default_v(d);
             r->row_lanes = d.tlr;
             r->block_threads = d.tbt;
+            r->count_mode = d.tcm + 1;
+            if (targets)
+                for (size_t k = 0; k < recs.size(); k++)
+                    if (bt[k * c.probs.size() + i] >= targets[gi]) {
+                        r->time_to_target_us = (double)recs[k].t_ns / 1000.0;
+                        r->steps_to_target = recs[k].steps;
+                        break;
+                    }
             stats(cut, r);
             r->time_us = ms * 1000.0;
             r->xi0 = c.xi0[i];
@@ -1133,7 +1178,8 @@ int sbx_destroy(sbx_ctx *ctx)
     Work &w = ctx->w;
     void *ptrs[] = {w.x, w.y, w.x2, w.S[0], w.S[1], w.Wp, w.fin, w.chg, w.newmask, w.stab, w.bif,
                     w.prev, w.ctl, w.wincount, w.visits, w.ab, w.sched, w.eacc, w.cut, w.trace,
-                    w.tours, w.valid, w.rjump, w.coef32, w.coef64, w.part, w.rinst, w.trace_t0};
+                    w.tours, w.valid, w.rjump, w.coef32, w.coef64, w.part, w.rinst, w.trace_t0,
+                    w.btrace, w.hcount};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
@@ -1313,7 +1359,8 @@ int sbx_solve(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
     if (p->ctx != ctx) return fail(ctx, SBX_ERR_ARG, "problem belongs to another (or a destroyed) context");
     if (pr->agents < 1 || pr->steps < 0 || !(pr->dt == pr->dt) || pr->precision < 0 ||
         pr->precision > 3 || pr->run_steps < 0 || pr->period < 0 || pr->threshold < 0 ||
-        pr->lane_agents < 0 || pr->row_lanes < 0 || pr->block_threads < 0 || !(pr->target == pr->target))
+        pr->lane_agents < 0 || pr->row_lanes < 0 || pr->block_threads < 0 || pr->count_mode < 0 ||
+        pr->count_mode > 2 || !(pr->target == pr->target))
         return fail(ctx, SBX_ERR_ARG, "bad params (agents >= 1, steps >= 0, precision 0..3)");
     if (pr->agents < 2 && !p->tsp) {
         // the reference's std dev divides by agents-1; one agent is allowed
@@ -1383,11 +1430,12 @@ int sbx_get_tours(sbx_ctx *ctx, int32_t *tours, int32_t *valid_step)
 }
 
 int sbx_solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const int32_t *agents,
-                    const sbx_params *params, sbx_result *res, double *agent_values, double *batch_time_us)
+                    const sbx_params *params, const double *targets, sbx_result *res,
+                    double *agent_values, double *batch_time_us)
 {
     if (!ctx) return fail(ctx, SBX_ERR_ARG, "null context");
     CK(cudaSetDevice(ctx->device));
-    return solve_batch(ctx, count, problems, agents, params, res, agent_values, batch_time_us);
+    return solve_batch(ctx, count, problems, agents, params, targets, res, agent_values, batch_time_us);
 }
 
 int sbx_get_trace(sbx_ctx *ctx, int64_t cap, int64_t *steps, double *best, double *t_us, int64_t *count)

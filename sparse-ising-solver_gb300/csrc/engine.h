@@ -20,9 +20,10 @@ struct RandInst {
     uint32_t V0[31];
 };
 
-// Rows with more neighbours than this are "heavy" (+-1 weights): a separate
-// kernel counts them in chunks of kHeavy; byte counters never overflow.
-constexpr int kHeavy = 128;
+// Rows with more neighbours than this are "heavy" (+-1 weights): the step
+// kernel counts them in chunks of kHeavy; byte counters (2 per neighbour)
+// never overflow.
+constexpr int kHeavy = 127;
 
 inline size_t prec_bytes(int p) { return p == P_F64 ? 8 : p == P_F32 ? 4 : 2; }
 
@@ -37,6 +38,7 @@ struct DevCsr {
     float *valf = nullptr;
     int32_t *perm = nullptr; // rows in decreasing degree (resident kernel order)
     bool skewed = false;     // max degree > 8x mean: the step kernel visits rows in perm order
+    int64_t nheavy = 0;      // heavy rows: the first nheavy entries of perm
     // Heavy rows (unit weights, degree > kHeavy) are split into chunks of
     // kHeavy neighbours whose partial counts a separate kernel computes.
     int32_t *hchunk = nullptr;    // per row: first chunk of a heavy row, else -1
@@ -47,6 +49,10 @@ struct DevCsr {
     float *c0r32 = nullptr;
     double *c0r64 = nullptr;
     int32_t *rinst = nullptr;
+    // batched: instances, their agent counts and weight sums (per-window trace)
+    int32_t ninst = 0;
+    int32_t *iagents = nullptr;
+    double *iwsum = nullptr;
     bool unit = false;       // all |w| == 1
     bool integer = false;    // all integer-valued, small enough for int32 sums
     double wsum = 0;         // reference csr.sum
@@ -80,10 +86,12 @@ struct Work {
     double2 *ab = nullptr;                // TSP (a_t, b_t) per step, FP64
     float2 *sched = nullptr;              // TSP (b_t, dt*-(1-a_t)) per step
     uint32_t *part = nullptr;             // heavy-row partial counts
+    int32_t *hcount = nullptr;            // heavy rows: finished chunks per (row, segment)
     unsigned long long *eacc = nullptr;   // per-agent cut accumulators
     double *cut = nullptr;                // per-agent cuts
     TraceRec *trace = nullptr;            // per-window records; trace_t0: loop start
     long long *trace_t0 = nullptr;
+    double *btrace = nullptr;             // batched: best cut [window][instance]
     int32_t *tours = nullptr, *valid = nullptr;
     uint32_t *rjump = nullptr;            // rand jump matrices (computed once)
     RandInst *rinst = nullptr;            // init instances of the current solve
@@ -92,7 +100,7 @@ struct Work {
     size_t cap_x = 0, cap_y = 0, cap_x2 = 0, cap_S0 = 0, cap_S1 = 0, cap_Wp = 0, cap_fin = 0,
            cap_chg = 0, cap_new = 0, cap_stab = 0, cap_bif = 0, cap_prev = 0, cap_ctl = 0,
            cap_win = 0, cap_visits = 0, cap_ab = 0, cap_sched = 0, cap_eacc = 0, cap_cut = 0,
-           cap_trace = 0, cap_t0 = 0, cap_tours = 0, cap_valid = 0, cap_rj = 0, cap_c32 = 0, cap_c64 = 0, cap_part = 0, cap_rinst = 0;
+           cap_trace = 0, cap_t0 = 0, cap_btrace = 0, cap_tours = 0, cap_valid = 0, cap_rj = 0, cap_c32 = 0, cap_c64 = 0, cap_part = 0, cap_rinst = 0, cap_hcount = 0;
     bool rjump_ready = false;
 };
 
@@ -109,7 +117,8 @@ struct SolveDims {
     // streaming step tile: agents per lane (0: widest vector that divides
     // Ap), lanes per row (32, 16, 8, 4), threads per CTA
     int32_t tv = 0, tlr = 32, tbt = 256;
-    int trace = 0;           // per-window best-cut records (streaming MaxCut)
+    int32_t tcm = 0;         // +-1 rows: 0 byte counters per lane, 1 bit planes per word
+    int trace = 0;           // per-window best-cut records: 1 one problem, 2 batched
 };
 
 // ---- launchers (k_*.cu) ----

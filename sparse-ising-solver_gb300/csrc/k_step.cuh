@@ -41,11 +41,14 @@ struct StepP {
     const int32_t *__restrict__ hchunk;   // heavy rows: first chunk, else -1
     const int32_t *__restrict__ chunk_row;
     uint2 *part;                          // [chunk][segment][lane] byte counters
-    const int32_t *__restrict__ order;    // skewed graphs: rows in decreasing degree
+    int32_t *hcount;                      // [first chunk][segment]: chunks of a heavy row done
+    const int32_t *__restrict__ order;    // rows in decreasing degree (or null: natural order)
+    int64_t row0;                         // first entry of order the row items visit
     const float *__restrict__ c0r32;      // batched: dt*xi0 per row (else null)
     const double *__restrict__ c0r64;
     int64_t n;
     int32_t W, Ap, nchunks;
+    int32_t stream_state;                 // state larger than L2: x, y loads/stores evict first
     double c0;
 };
 
@@ -84,6 +87,20 @@ template <class T, int V> __device__ __forceinline__ Raw<V * sizeof(T)> vload(co
     Raw<V * sizeof(T)> r;
     r.u = *(const decltype(r.u) *)p;
     return r;
+}
+// State passes that do not fit in L2 stream through it: loads and stores
+// marked evict-first keep the sign planes (the gathered data) resident.
+template <class T, int V> __device__ __forceinline__ Raw<V * sizeof(T)> vload_s(const T *p, bool cs)
+{
+    Raw<V * sizeof(T)> r;
+    if (cs) r.u = __ldcs((const decltype(r.u) *)p);
+    else r.u = *(const decltype(r.u) *)p;
+    return r;
+}
+template <class U> __device__ __forceinline__ void vstore_s(void *p, const U &u, bool cs)
+{
+    if (cs) __stcs((U *)p, u);
+    else *(U *)p = u;
 }
 template <class T, int V> __device__ __forceinline__ void unpack(const Raw<V * sizeof(T)> &r, T (&o)[V])
 {
@@ -148,70 +165,200 @@ __device__ __forceinline__ Raw<V * sizeof(T)> from_vals(const A (&o)[V])
     return r;
 }
 
-// Partial counts of heavy rows (+-1 weights): item = (chunk of kHeavy
-// neighbours, segment of 32*V agents); a lane leaves the byte counters of its
-// V agents, which the step kernel then sums for the row.
-template <int V>
-__global__ void __launch_bounds__(256) k_heavy(const StepP P, const int offset)
-{
-    pdl_wait();
-    if (P.ctl[CTL_STOP]) return;
-    const int step = P.ctl[CTL_STEP] + offset;
-    pdl_trigger();
-    const int lane = threadIdx.x & 31;
-    const uint32_t *Scur = (step & 1) ? P.S1 : P.S0;
-    const int nit = P.Ap / (32 * V);
-    const int64_t items = (int64_t)P.nchunks * nit;
-    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t item = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); item < items;
-         item += nw) {
-        const int c = (int)(item / nit), it = (int)(item - (int64_t)c * nit);
-        const int32_t r = __ldg(&P.chunk_row[c]);
-        const int32_t e0 = __ldg(&P.rowptr[r]) + (c - __ldg(&P.hchunk[r])) * kHeavy;
-        const int32_t e1 = min(__ldg(&P.rowptr[r + 1]), e0 + kHeavy);
-        const int a0 = it * 32 * V + lane * V;
-        const int q = a0 >> 5, off = a0 & 31;
-        const uint32_t *Sq = Scur + q;
-        uint32_t lo = 0, hi = 0;
-        for (int32_t cb = e0; cb < e1; cb += 32) {
-            const int m = min(32, e1 - cb);
-            const uint32_t mycw = lane < m ? __ldg(&P.colw[cb + lane]) : 0u;
-#pragma unroll 4
-            for (int k = 0; k < m; k++) {
-                const uint32_t cw = __shfl_sync(FULL, mycw, k);
-                uint32_t bits = __ldg(Sq + (size_t)(cw & 0x7fffffffu) * (size_t)P.W) >> off;
-                bits ^= (uint32_t)((int32_t)cw >> 31);
-                lo += spread4(bits & 0xfu);
-                if (V == 8) hi += spread4((bits >> 4) & 0xfu);
-            }
-        }
-        P.part[item * 32 + lane] = make_uint2(lo, hi);
-    }
-}
-
-// One SB step over every (row, agent).  Work item = (row, segment of 32*V
-// agents); a warp takes items in turn, lane l owns V consecutive agents of the
-// segment (one vector load of x and of y).  Per neighbour j the lane reads the
-// sign word of its agents in row j of the plane (lanes of one word share the
-// address), XORs the weight's sign and adds the V bits into byte counters
-// (bit i of a nibble lands in byte i after multiplying by 0x00204081); the
-// force is 2*count - degree, exact (src/kernels.cu:247-255).  A byte counter
-// holds up to kHeavy = 128 neighbours; longer rows (+-1 weights) are counted
-// in kHeavy chunks by k_heavy and the BIG kernels add those partials.
-// The new signs of the V agents are OR-combined across the lanes of a word
-// and written once.
 // x + a*b: one FMA in FP32; in FP64 two separately rounded operations, the
 // reference's arithmetic as the oracle states it.
 __device__ __forceinline__ float madd(float a, float b, float x) { return fmaf(a, b, x); }
 __device__ __forceinline__ double madd(double a, double b, double x) { return __dadd_rn(x, __dmul_rn(a, b)); }
 
-template <class T, int V, int KIND, bool WIN, int WM, bool BIG, int LR>
-__global__ void __launch_bounds__(256) k_row(const StepP P, const int offset)
+// Twice the sign bits of a nibble, one per byte: byte i of the result is
+// 2 * bit i.  Byte counters of +-1 neighbours then hold 2 * count (<= 254 for
+// up to kHeavy = 127 neighbours).
+__device__ __forceinline__ uint32_t spread2x(uint32_t nib) { return (nib * 0x00408102u) & 0x02020202u; }
+
+// Walk m neighbours (+-1 weights) of one row starting at CSR entry e0, all 32
+// lanes of the warp together: lane l reads the sign word of its V agents in
+// each neighbour's row of the plane and adds 2 * (bit ^ weight sign) into
+// byte counters lo (agents 0..3) / hi (4..7).  Counts agents whose neighbour
+// term is -1: the force is 2 * count - degree (src/kernels.cu:247-255).
+template <int V, int LR>
+__device__ __forceinline__ void count_unit(const StepP &P, const uint32_t *Sq, int off, int32_t e0,
+                                           int32_t dw, int sl, uint32_t &lo, uint32_t &hi)
 {
-    static_assert(LR == 32 || !BIG, "heavy-row partials are laid out for whole-warp rows");
+    int32_t dmax = dw;
+    if constexpr (LR < 32) dmax = __reduce_max_sync(FULL, dw);
+    for (int32_t cb = 0; cb < dmax; cb += LR) {
+        const int m = min(LR, dmax - cb);
+        const int32_t idx = cb + sl;
+        const uint32_t mycw = idx < dw ? __ldg(&P.colw[e0 + idx]) : 0u;
+#pragma unroll 4
+        for (int k = 0; k < m; k++) {
+            const uint32_t cw = __shfl_sync(FULL, mycw, k, LR);
+            if (LR == 32 || cb + k < dw) {
+                const uint32_t word = __ldg(Sq + (size_t)(cw & 0x7fffffffu) * (size_t)P.W);
+                // weight sign -> all-ones mask; unused high bits only reach
+                // counter bytes that are never read
+                const uint32_t bits = (word >> off) ^ (uint32_t)((int32_t)cw >> 31);
+                lo += spread2x(bits & 0xfu);
+                if (V == 8) hi += spread2x((bits >> 4) & 0xfu);
+            }
+        }
+    }
+}
+
+// Bit-sliced counting of the same quantity for rows with many neighbours:
+// the G = 32/V lanes sharing a sign word split the row's neighbours (lane j
+// of the group takes every G-th); each adds whole 32-agent words (bit ^
+// weight sign) into bit planes -- bit a of plane i is bit i of agent a's
+// count -- with a ripple of two logic operations per plane.  The planes are
+// then summed across the group (butterfly of shuffles and bit-sliced adds)
+// and each lane takes out its V agents as byte counters holding 2 * count,
+// the form count_unit leaves.  Counts stay below 128 (kHeavy = 127).
+template <int V, int LR>
+__device__ __forceinline__ void count_bits(const StepP &P, const uint32_t *Sq, int off, int32_t e0,
+                                           int32_t dw, int sl, uint32_t &lo, uint32_t &hi)
+{
+    constexpr int G = 32 / V;
+    static_assert(LR % G == 0, "a row's lanes hold whole words");
+    // planes one lane needs for ceil(127 / G) neighbours; 7 after the sum
+    constexpr int BL = G == 4 ? 6 : G == 8 ? 5 : G == 16 ? 4 : 3;
+    constexpr int NP = 7;
+    const int j = sl & (G - 1);
+    uint32_t p[NP];
+#pragma unroll
+    for (int i = 0; i < NP; i++) p[i] = 0;
+    int32_t dmax = dw;
+    if constexpr (LR < 32) dmax = __reduce_max_sync(FULL, dw);
+    for (int32_t cb = 0; cb < dmax; cb += LR) {
+        const int32_t idx = cb + sl;
+        const uint32_t mycw = idx < dw ? __ldg(&P.colw[e0 + idx]) : 0u;
+        const int m = min(LR, dmax - cb);
+        for (int k = 0; k < m; k += G) {
+            const int src = k + j;
+            const uint32_t cw = __shfl_sync(FULL, mycw, src, LR);
+            // past the row's end cw is 0: the load reads row 0, the term is dropped
+            const uint32_t w = __ldg(Sq + (size_t)(cw & 0x7fffffffu) * (size_t)P.W);
+            uint32_t c = (cb + src < dw) ? (w ^ (uint32_t)((int32_t)cw >> 31)) : 0u;
+#pragma unroll
+            for (int i = 0; i < BL; i++) {
+                const uint32_t t = p[i] & c;
+                p[i] ^= c;
+                c = t;
+            }
+        }
+    }
+    // sum over the group: planes grow by one per round, capped at 7
+#pragma unroll
+    for (int s = 1, np = BL; s < G; s <<= 1, np = np + 1 < NP ? np + 1 : NP) {
+        uint32_t c = 0;
+#pragma unroll
+        for (int i = 0; i < NP; i++) {
+            if (i <= np) {
+                const uint32_t a = p[i], b = __shfl_xor_sync(FULL, p[i], s);
+                p[i] = a ^ b ^ c;
+                c = (a & b) | (c & (a ^ b));
+            }
+        }
+    }
+    // this lane's V agents: bit k of plane i -> 2^(i+1) in byte k
+#pragma unroll
+    for (int i = 0; i < NP; i++) {
+        const uint32_t b = p[i] >> off;
+        lo += ((b & 0xfu) * (0x00204081u << (i + 1))) & (0x01010101u << (i + 1));
+        if (V == 8) hi += (((b >> 4) & 0xfu) * (0x00204081u << (i + 1))) & (0x01010101u << (i + 1));
+    }
+}
+
+// The SB update of V agents from their totals (the force sum_j J_ij s_j):
+// src/kernels.cu:236-262 in the fused mode -- clamp or kick, then the drift /
+// kick pair that runs unconditionally, so a clamped oscillator leaves with
+// y = dt (p-1) sign(x) -- or the unfused trio's mat_mult (:207) and confine
+// (:158-165), then Update_XY of the next step unless the window closes.
+// FP32 pairs go through the packed FMA (per component the same rounding as
+// fmaf); FP64 keeps separately rounded operations.
+template <int KIND, bool WIN, int V, class C4>
+__device__ __forceinline__ void sb_update(float (&x)[V], float (&y)[V], const float (&tv)[V], float c0,
+                                          const C4 &c, const C4 &cn)
+{
+    if constexpr (V % 2 == 0) {
+        const float2 c02 = make_float2(c0, c0);
+#pragma unroll
+        for (int i = 0; i < V; i += 2) {
+            float2 X = make_float2(x[i], x[i + 1]), Y = make_float2(y[i], y[i + 1]);
+            const float2 K = __ffma2_rn(c02, make_float2(tv[i], tv[i + 1]), Y);
+            const bool k0 = fabsf(X.x) > 1.0f, k1 = fabsf(X.y) > 1.0f;
+            Y.x = k0 ? 0.0f : K.x;
+            Y.y = k1 ? 0.0f : K.y;
+            X.x = k0 ? spin_of(X.x) : X.x;
+            X.y = k1 ? spin_of(X.y) : X.y;
+            if (KIND == K_FUSED) {
+                X = __ffma2_rn(make_float2(c.x, c.x), Y, X);
+                Y = __ffma2_rn(make_float2(c.y, c.y), X, Y);
+            } else if (!WIN) {
+                Y = __ffma2_rn(make_float2(cn.w, cn.w), X, Y);
+                X = __ffma2_rn(make_float2(cn.z, cn.z), Y, X);
+            }
+            x[i] = X.x;
+            x[i + 1] = X.y;
+            y[i] = Y.x;
+            y[i + 1] = Y.y;
+        }
+    } else {
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+            const bool clamp = fabsf(x[v]) > 1.0f;
+            const float xc = spin_of(x[v]);
+            y[v] = clamp ? 0.0f : fmaf(c0, tv[v], y[v]);
+            x[v] = clamp ? xc : x[v];
+            if (KIND == K_FUSED) {
+                x[v] = fmaf(c.x, y[v], x[v]);
+                y[v] = fmaf(c.y, x[v], y[v]);
+            } else if (!WIN) {
+                y[v] = fmaf(cn.w, x[v], y[v]);
+                x[v] = fmaf(cn.z, y[v], x[v]);
+            }
+        }
+    }
+}
+template <int KIND, bool WIN, int V, class C4>
+__device__ __forceinline__ void sb_update(double (&x)[V], double (&y)[V], const double (&tv)[V], double c0,
+                                          const C4 &c, const C4 &cn)
+{
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+        const bool clamp = fabs(x[v]) > 1.0;
+        const double xc = spin_of(x[v]);
+        y[v] = clamp ? 0.0 : madd(c0, tv[v], y[v]);
+        x[v] = clamp ? xc : x[v];
+        if (KIND == K_FUSED) {
+            x[v] = madd(c.x, y[v], x[v]);
+            y[v] = madd(c.y, x[v], y[v]);
+        } else if (!WIN) {
+            y[v] = madd(cn.w, x[v], y[v]);
+            x[v] = madd(cn.z, y[v], x[v]);
+        }
+    }
+}
+
+// One SB step over every (row, agent).  Work item = (group of 32/LR rows,
+// segment of LR*V agents); lane l of a row owns V consecutive agents (one
+// vector load of x and of y).  Per neighbour j the lane reads the sign word
+// of its agents in row j of the plane (lanes of one word share the address)
+// and counts into byte counters (count_unit); the new signs of the V agents
+// are OR-combined across the lanes of a word and written once.
+//
+// Heavy rows (BIG kernels: +-1 weights, degree > kHeavy) come first, as
+// items of kHeavy neighbours: each leaves its byte counters in P.part, and
+// the warp completing a row's last chunk (a per-row counter, re-armed by that
+// warp) sums them and updates the row.  The other rows follow, in decreasing
+// degree when P.order is set.
+template <class T, int V, int KIND, bool WIN, int WM, bool BIG, int LR, int CM>
+__global__ void __launch_bounds__(256, BIG ? 6 : 1) k_row(const StepP P, const int offset)
+{
+    static_assert(LR == 32 || !BIG, "heavy rows are counted by whole warps");
     static_assert(LR * V >= 32, "a sign word belongs to one row's lanes");
     using A = typename St<T>::A;
     using R = typename std::conditional<WM == W_F64, double, float>::type;
+    using RawT = Raw<V * sizeof(T)>;
     extern __shared__ uint32_t s_chg[];   // [W] window steps: changed bits of this block
     pdl_wait();
     if (P.ctl[CTL_STOP]) return;          // block-uniform
@@ -223,175 +370,47 @@ __global__ void __launch_bounds__(256) k_row(const StepP P, const int offset)
     }
     pdl_trigger();
     T *xp = (T *)P.x, *yp = (T *)P.y;
+    const bool cs = P.stream_state != 0;
+    // coefficients of this step and of the next (the unfused mode's
+    // Update_XY), loop-invariant
+    const auto c = Coef<A>::get(P, step);
+    const auto cn = Coef<A>::get(P, step + 1);
     uint32_t *Scur = (step & 1) ? P.S1 : P.S0;
     uint32_t *Snext = (step & 1) ? P.S0 : P.S1;
     constexpr int G = 32 / V;   // lanes sharing one sign word
-    constexpr int RW = 32 / LR; // rows per warp: LR lanes per row
+    constexpr int RW = 32 / LR; // rows per warp
     constexpr uint32_t VM = (V == 32) ? 0xffffffffu : ((1u << V) - 1u);
     const int rw = lane / LR, sl = lane & (LR - 1);   // row of the warp, lane of the row
-    // Items (group of RW rows, segment of LR*V agents) in steps of the warp
-    // count, advanced without divisions: g += nw / nit, it += nw % nit with
-    // carry.  Below 32 lanes per row a row is one segment (nit = 1).
-    const int nit = P.Ap / (LR * V);
-    const int64_t ng = (P.n + RW - 1) / RW;
+    const int nit = P.Ap / (LR * V);                  // segments per row (1 when LR < 32)
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
     const int64_t w0 = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int64_t dr = nw / nit;
-    const int dit = (int)(nw - dr * nit);
-    int64_t g = w0 / nit;
-    int it = (int)(w0 - g * nit);
-    for (; g < ng; g += dr, it += dit) {
-        if (it >= nit) {
-            it -= nit;
-            g++;
-            if (g >= ng) break;
-        }
-        // Lanes of a group past the last row repeat row n-1 and store nothing.
-        const int64_t gi = g * RW + rw;
-        const bool live = RW == 1 || gi < P.n;
-        const int64_t ri = live ? gi : P.n - 1;
-        // Skewed graphs are visited in decreasing degree, so every warp's
-        // share holds the same mix of long and short rows.
-        const int64_t r = P.order ? (int64_t)__ldg(&P.order[ri]) : ri;
-        const int a0 = it * LR * V + sl * V;
-        const int q = a0 >> 5, off = a0 & 31;
-        const int64_t base = r * P.Ap + a0;
-        uint32_t wp_old = 0;   // window steps: the previous window's word, fetched early
-        if (WIN && (lane & (G - 1)) == 0) wp_old = P.Wp[r * P.W + q];
-        const auto xr = vload<T, V>(xp + base);
-        const auto yr = vload<T, V>(yp + base);
+
+    // The item's update from the totals tv of its agents; x, y stored, the
+    // new sign word written (and compared with the previous window's).
+    auto finish = [&](int64_t r, int q, int off, int64_t base, bool live, const RawT &xr, const RawT &yr,
+                      const A (&tv)[V], A c0, uint32_t wp_old) {
         A x[V], y[V];
+        to_vals<T, V>(xr, x);
+        to_vals<T, V>(yr, y);
         if (KIND == K_XY) {
             // Update_XY, src/kernels.cu:8-22 (pressure not clamped)
-            const auto c = Coef<A>::get(P, step);
-            to_vals<T, V>(xr, x);
-            to_vals<T, V>(yr, y);
 #pragma unroll
             for (int v = 0; v < V; v++) {
                 y[v] = madd((A)c.w, x[v], y[v]);
                 x[v] = madd((A)c.z, y[v], x[v]);
             }
         } else {
-            const int32_t e0 = __ldg(&P.rowptr[r]), e1 = __ldg(&P.rowptr[r + 1]);
-            const int deg = e1 - e0;
-            uint32_t lo = 0, hi = 0;
-            int cnt[BIG ? V : 1];
-            R tot[WM == W_UNIT ? 1 : V];
-#pragma unroll
-            for (int v = 0; v < (BIG ? V : 1); v++) cnt[v] = 0;
-#pragma unroll
-            for (int v = 0; v < (WM == W_UNIT ? 1 : V); v++) tot[v] = R(0);
-            // Heavy rows (BIG kernels only) take their counts from k_heavy.
-            // With several rows per warp the walk runs to the longest row of
-            // the warp; shuffles stay warp-wide, loads and sums per row.
-            const int32_t dw = (BIG && WM == W_UNIT && deg > kHeavy) ? 0 : deg;
-            int32_t dmax = dw;
-            if constexpr (LR < 32) dmax = __reduce_max_sync(FULL, dw);
-            for (int32_t cb = 0; cb < dmax; cb += LR) {
-                const int m = min(LR, dmax - cb);
-                const int32_t idx = cb + sl;
-                const uint32_t mycw = idx < dw ? __ldg(&P.colw[e0 + idx]) : 0u;
-                R myv = R(0);
-                if (WM == W_F32) myv = idx < dw ? __ldg(&P.valf[e0 + idx]) : 0.f;
-                if (WM == W_F64) myv = idx < dw ? __ldg(&P.vald[e0 + idx]) : 0.0;
-                const uint32_t *Sq = Scur + q;
-#pragma unroll 4
-                for (int k = 0; k < m; k++) {
-                    const uint32_t cw = __shfl_sync(FULL, mycw, k, LR);
-                    R wv = R(0);
-                    if (WM != W_UNIT) wv = __shfl_sync(FULL, myv, k, LR);
-                    if (LR == 32 || cb + k < dw) {
-                        const uint32_t word = __ldg(Sq + (size_t)(cw & 0x7fffffffu) * (size_t)P.W);
-                        uint32_t bits = word >> off;
-                        if (WM == W_UNIT) {
-                            // weight sign -> all-ones mask; unused high bits
-                            // only reach counter bytes that are never read
-                            bits ^= (uint32_t)((int32_t)cw >> 31);
-                            lo += spread4(bits & 0xfu);
-                            if (V == 8) hi += spread4((bits >> 4) & 0xfu);
-                        } else {
-                            bits &= VM;
-#pragma unroll
-                            for (int v = 0; v < V; v++) {
-                                const R sv = ((bits >> v) & 1u) ? R(-1) : R(1);
-                                if (WM == W_F64) tot[v] = sub(tot[v], mul(wv, sv));
-                                else tot[v] -= wv * sv;
-                            }
-                        }
-                    }
-                }
-            }
-            if (BIG && WM == W_UNIT) {
-                if (deg > kHeavy) {
-                    // a heavy row: its neighbours were counted in chunks by
-                    // k_heavy; the loop above did not run for it
-                    const int c0i = __ldg(&P.hchunk[r]), nc = (deg + kHeavy - 1) / kHeavy;
-                    for (int cc = 0; cc < nc; cc++) {
-                        const uint2 pr = P.part[((int64_t)(c0i + cc) * nit + it) * 32 + lane];
-#pragma unroll
-                        for (int v = 0; v < (BIG ? V : 1); v++)
-                            cnt[v] += ((v < 4 ? pr.x : pr.y) >> (8 * (v & 3))) & 0xffu;
-                    }
-                } else {
-#pragma unroll
-                    for (int v = 0; v < (BIG ? V : 1); v++)
-                        cnt[v] += ((v < 4 ? lo : hi) >> (8 * (v & 3))) & 0xffu;
-                }
-            }
-            const auto c = Coef<A>::get(P, step);
-            A c0 = (A)P.c0;
-            if (P.c0r32) c0 = std::is_same<A, double>::value ? (A)__ldg(&P.c0r64[r]) : (A)__ldg(&P.c0r32[r]);
-            // FP32 totals straight from the byte counters: PRMT builds the
-            // float 2^23 + count; fma(2, f, -2^24) is 2*count exactly, and
-            // subtracting the degree gives the exact integer 2*count - deg.
-            const float fdeg = (float)deg;
-            to_vals<T, V>(xr, x);
-            to_vals<T, V>(yr, y);
-#pragma unroll
-            for (int v = 0; v < V; v++) {
-                A total;
-                if (WM != W_UNIT) {
-                    total = (A)tot[WM == W_UNIT ? 0 : v];
-                } else if (BIG) {
-                    total = (A)(2 * cnt[v < (BIG ? V : 1) ? v : 0] - deg);
-                } else if (std::is_same<A, float>::value) {
-                    const uint32_t f = __byte_perm(v < 4 ? lo : hi, 0x4b000000u, 0x7440u + (v & 3));
-                    total = (A)(fmaf(2.0f, __uint_as_float(f), -16777216.0f) - fdeg);
-                } else {
-                    total = (A)(2 * (int)(((v < 4 ? lo : hi) >> (8 * (v & 3))) & 0xffu) - deg);
-                }
-                const bool clamp = fabs(x[v]) > A(1);
-                const A xc = spin_of(x[v]);
-                if (KIND == K_FUSED) {
-                    // src/kernels.cu:236-262: clamp or kick, then the drift /
-                    // kick pair that runs unconditionally (a clamped oscillator
-                    // leaves with y = dt (p-1) sign(x)).
-                    y[v] = clamp ? A(0) : madd(c0, total, y[v]);
-                    x[v] = clamp ? xc : x[v];
-                    x[v] = madd((A)c.x, y[v], x[v]);
-                    y[v] = madd((A)c.y, x[v], y[v]);
-                } else {
-                    // mat_mult (:207) and confine (:158-165) of this step, then
-                    // Update_XY of the next one unless the window closes here.
-                    y[v] = clamp ? A(0) : madd(c0, total, y[v]);
-                    x[v] = clamp ? xc : x[v];
-                    if (!WIN) {
-                        const auto cn = Coef<A>::get(P, step + 1);
-                        y[v] = madd((A)cn.w, x[v], y[v]);
-                        x[v] = madd((A)cn.z, y[v], x[v]);
-                    }
-                }
-            }
+            sb_update<KIND, WIN, V>(x, y, tv, c0, c, cn);
         }
-        // Signs of the new x (rounding to the storage type keeps the sign).
+        // signs of the new x (rounding to the storage type keeps the sign)
         uint32_t b = 0;
 #pragma unroll
         for (int v = 0; v < V; v++) b |= sbit(x[v]) << v;
         const auto xw = from_vals<T, V>(x);
         const auto yw = from_vals<T, V>(y);
         if (live) {
-            *(decltype(xw.u) *)(xp + base) = xw.u;
-            *(decltype(yw.u) *)(yp + base) = yw.u;
+            vstore_s(xp + base, xw.u, cs);
+            vstore_s(yp + base, yw.u, cs);
         }
         b <<= off;
 #pragma unroll
@@ -407,6 +426,135 @@ __global__ void __launch_bounds__(256) k_row(const StepP P, const int offset)
                 if (ch) atomicOr(&s_chg[q], ch);
             }
         }
+    };
+    // dt * xi0 of the row's instance (batched) or of the problem
+    auto row_c0 = [&](int64_t r) -> A {
+        if (P.c0r32) return std::is_same<A, double>::value ? (A)__ldg(&P.c0r64[r]) : (A)__ldg(&P.c0r32[r]);
+        return (A)P.c0;
+    };
+
+    if constexpr (BIG) {
+        const int64_t hitems = (int64_t)P.nchunks * nit;
+        for (int64_t item = w0; item < hitems; item += nw) {
+            const int ci = (int)(item / nit), it = (int)(item - (int64_t)ci * nit);
+            const int64_t r = __ldg(&P.chunk_row[ci]);
+            const int32_t h0 = __ldg(&P.hchunk[r]);
+            const int32_t rb = __ldg(&P.rowptr[r]), re = __ldg(&P.rowptr[r + 1]);
+            const int32_t e0 = rb + (ci - h0) * kHeavy;
+            const int a0 = it * 32 * V + lane * V;
+            const int q = a0 >> 5, off = a0 & 31;
+            uint32_t lo = 0, hi = 0;
+            count_bits<V, 32>(P, Scur + q, off, e0, min(re - e0, (int32_t)kHeavy), lane, lo, hi);
+            P.part[item * 32 + lane] = make_uint2(lo, hi);
+            // publish the partial, then count the row's finished chunks
+            __threadfence();
+            const int deg = re - rb, nc = (deg + kHeavy - 1) / kHeavy;
+            int last = 0;
+            if (lane == 0) last = atomicAdd(&P.hcount[(int64_t)h0 * nit + it], 1) == nc - 1;
+            if (!__shfl_sync(FULL, last, 0)) continue;   // warp-uniform
+            __threadfence();
+            if (lane == 0) P.hcount[(int64_t)h0 * nit + it] = 0;   // armed for the next step
+            int s[V];
+#pragma unroll
+            for (int v = 0; v < V; v++) s[v] = 0;
+            for (int cc = 0; cc < nc; cc++) {
+                const uint2 pr = __ldcg(&P.part[((int64_t)(h0 + cc) * nit + it) * 32 + lane]);
+#pragma unroll
+                for (int v = 0; v < V; v++) s[v] += ((v < 4 ? pr.x : pr.y) >> (8 * (v & 3))) & 0xffu;
+            }
+            A tv[V];
+#pragma unroll
+            for (int v = 0; v < V; v++) tv[v] = (A)(s[v] - deg);
+            const int64_t base = r * P.Ap + a0;
+            uint32_t wp_old = 0;
+            if (WIN && (lane & (G - 1)) == 0) wp_old = P.Wp[r * P.W + q];
+            const RawT xr = vload_s<T, V>(xp + base, cs);
+            const RawT yr = vload_s<T, V>(yp + base, cs);
+            finish(r, q, off, base, true, xr, yr, tv, row_c0(r), wp_old);
+        }
+    }
+
+    // Row items (group g, segment it) in steps of the warp count, advanced
+    // without divisions: g += nw / nit, it += nw % nit with carry.
+    const int64_t nrows = P.n - P.row0;
+    const int64_t ng = (nrows + RW - 1) / RW;
+    const int64_t dr = nw / nit;
+    const int dit = (int)(nw - dr * nit);
+    int64_t g = w0 / nit;
+    int it = (int)(w0 - g * nit);
+    for (; g < ng; g += dr, it += dit) {
+        if (it >= nit) {
+            it -= nit;
+            g++;
+            if (g >= ng) break;
+        }
+        // lanes of a group past the last row repeat the last row, store nothing
+        const int64_t gi = g * RW + rw;
+        const bool live = RW == 1 || gi < nrows;
+        const int64_t ri = P.row0 + (live ? gi : nrows - 1);
+        const int64_t r = P.order ? (int64_t)__ldg(&P.order[ri]) : ri;
+        const int a0 = it * LR * V + sl * V;
+        const int q = a0 >> 5, off = a0 & 31;
+        const int64_t base = r * P.Ap + a0;
+        uint32_t wp_old = 0;   // window steps: the previous window's word, fetched early
+        if (WIN && (lane & (G - 1)) == 0) wp_old = P.Wp[r * P.W + q];
+        const RawT xr = vload_s<T, V>(xp + base, cs);
+        const RawT yr = vload_s<T, V>(yp + base, cs);
+        A tv[V];
+        if (KIND != K_XY) {
+            const int32_t e0 = __ldg(&P.rowptr[r]), e1 = __ldg(&P.rowptr[r + 1]);
+            const int32_t deg = e1 - e0;
+            if (WM == W_UNIT) {
+                uint32_t lo = 0, hi = 0;
+                if (CM) count_bits<V, LR>(P, Scur + q, off, e0, deg, sl, lo, hi);
+                else count_unit<V, LR>(P, Scur + q, off, e0, deg, sl, lo, hi);
+                if constexpr (std::is_same<A, float>::value) {
+                    // PRMT builds the float 2^23 + 2*count from a byte
+                    // counter; minus (2^23 + deg) it is 2*count - deg exactly
+                    const float bias = 8388608.0f + (float)deg;
+#pragma unroll
+                    for (int v = 0; v < V; v++)
+                        tv[v] = __uint_as_float(__byte_perm(v < 4 ? lo : hi, 0x4b000000u, 0x7440u + (v & 3))) - bias;
+                } else {
+#pragma unroll
+                    for (int v = 0; v < V; v++)
+                        tv[v] = (A)((int)(((v < 4 ? lo : hi) >> (8 * (v & 3))) & 0xffu) - deg);
+                }
+            } else {
+                R tot[V];
+#pragma unroll
+                for (int v = 0; v < V; v++) tot[v] = R(0);
+                int32_t dmax = deg;
+                if constexpr (LR < 32) dmax = __reduce_max_sync(FULL, deg);
+                const uint32_t *Sq = Scur + q;
+                for (int32_t cb = 0; cb < dmax; cb += LR) {
+                    const int m = min(LR, dmax - cb);
+                    const int32_t idx = cb + sl;
+                    const uint32_t mycw = idx < deg ? __ldg(&P.colw[e0 + idx]) : 0u;
+                    R myv = R(0);
+                    if (WM == W_F32) myv = idx < deg ? __ldg(&P.valf[e0 + idx]) : 0.f;
+                    if (WM == W_F64) myv = idx < deg ? __ldg(&P.vald[e0 + idx]) : 0.0;
+#pragma unroll 4
+                    for (int k = 0; k < m; k++) {
+                        const uint32_t cw = __shfl_sync(FULL, mycw, k, LR);
+                        const R wv = __shfl_sync(FULL, myv, k, LR);
+                        if (LR == 32 || cb + k < deg) {
+                            const uint32_t word = __ldg(Sq + (size_t)(cw & 0x7fffffffu) * (size_t)P.W);
+                            const uint32_t bits = (word >> off) & VM;
+#pragma unroll
+                            for (int v = 0; v < V; v++) {
+                                const R sv = ((bits >> v) & 1u) ? R(-1) : R(1);
+                                if (WM == W_F64) tot[v] = sub(tot[v], mul(wv, sv));
+                                else tot[v] -= wv * sv;
+                            }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int v = 0; v < V; v++) tv[v] = (A)tot[v];
+            }
+        }
+        finish(r, q, off, base, live, xr, yr, tv, row_c0(r), wp_old);
     }
     if (WIN) {
         __syncthreads();
@@ -459,26 +607,43 @@ template <class T, int V, int LR, int KIND, bool WIN>
 cudaError_t step_vl(const SolveDims &d, const DevCsr &J, const StepP &P, int offset, cudaStream_t s)
 {
     constexpr int RW = 32 / LR;
-    const int64_t items = (d.n + RW - 1) / RW * (d.Ap / (LR * V));
     const size_t smem = WIN ? sizeof(uint32_t) * d.W : 0;
     const int bt = d.tbt;
+    const int nit = d.Ap / (LR * V);
     const bool big = J.unit && J.nchunks > 0 && KIND != K_XY;
+    // Row order: heavy rows first (their chunk items), then the rest in
+    // decreasing degree when rows differ much in length or share a warp.
+    StepP Q = P;
+    Q.order = nullptr;
+    Q.row0 = 0;
+    if (big) {
+        Q.order = J.perm;
+        Q.row0 = J.nheavy;
+    } else if (KIND != K_XY && (J.skewed || LR < 32)) {
+        Q.order = J.perm;
+    }
+    const int64_t items = ((d.n - Q.row0 + RW - 1) / RW + (big ? J.nchunks : 0)) * nit;
+    // count mode of the +-1 rows: byte counters per lane (0) or bit planes (1)
+    const bool cm = d.tcm != 0;
     if constexpr (LR == 32) {
         if (big) {
-            cudaError_t e = launch_grid(k_heavy<V>, d, (int64_t)J.nchunks * (d.Ap / (32 * V)), 256, 0, s, P,
-                                        offset);
-            if (e != cudaSuccess) return e;
-            return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, true, 32>, d, items, bt, smem, s, P, offset);
+            if (cm) return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, true, 32, 1>, d, items, bt, smem, s, Q, offset);
+            return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, true, 32, 0>, d, items, bt, smem, s, Q, offset);
         }
     } else {
         if (big) return cudaErrorInvalidValue;
     }
-    if (KIND == K_XY || J.unit)
-        return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, false, LR>, d, items, bt, smem, s, P, offset);
+    if (KIND == K_XY) return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, false, LR, 0>, d, items, bt, smem, s, Q, offset);
+    if (J.unit) {
+        if constexpr (KIND != K_XY) {
+            if (cm) return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, false, LR, 1>, d, items, bt, smem, s, Q, offset);
+        }
+        return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, false, LR, 0>, d, items, bt, smem, s, Q, offset);
+    }
     if constexpr (sizeof(T) == 8)
-        return launch_grid(k_row<T, V, KIND, WIN, W_F64, false, LR>, d, items, bt, smem, s, P, offset);
+        return launch_grid(k_row<T, V, KIND, WIN, W_F64, false, LR, 0>, d, items, bt, smem, s, Q, offset);
     else
-        return launch_grid(k_row<T, V, KIND, WIN, W_F32, false, LR>, d, items, bt, smem, s, P, offset);
+        return launch_grid(k_row<T, V, KIND, WIN, W_F32, false, LR, 0>, d, items, bt, smem, s, Q, offset);
 }
 
 // Agents per lane by default: a 16-byte vector when the padded agent count

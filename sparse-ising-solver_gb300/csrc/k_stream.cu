@@ -109,6 +109,41 @@ __global__ void __launch_bounds__(256) k_trace_window(const double *__restrict__
     }
 }
 
+// Batched record of the window that just closed (every window closes: the
+// batched solve has no early exit): block i writes instance i's best cut,
+// -0.5 * (0.5 * E - W_i) exactly (src/kernels.cu:383-398); block 0 the
+// window's steps and time.
+__global__ void __launch_bounds__(64) k_trace_batch(const unsigned long long *__restrict__ eacc,
+                                                    int32_t Ap, const int32_t *__restrict__ agents,
+                                                    const double *__restrict__ wsum, int32_t ninst,
+                                                    const int32_t *ctl, TraceRec *rec, double *best,
+                                                    const long long *t0, int64_t cap)
+{
+    const int i = blockIdx.x;
+    const int win = ctl[CTL_WINDOWS] - 1;
+    if (win < 0 || win >= cap) return;   // block-uniform
+    double b = -INFINITY;
+    for (int a = threadIdx.x; a < agents[i]; a += blockDim.x) {
+        const double tmp = 0.5 * (double)(long long)eacc[(int64_t)i * Ap + a];
+        b = fmax(b, __dmul_rn(-0.5, __dsub_rn(tmp, wsum[i])));
+    }
+    for (int o = 16; o; o >>= 1) b = fmax(b, __shfl_xor_sync(FULL, b, o));
+    __shared__ double wb[2];
+    if ((threadIdx.x & 31) == 0) wb[threadIdx.x >> 5] = b;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        best[(int64_t)win * ninst + i] = fmax(wb[0], wb[1]);
+        if (i == 0) {
+            TraceRec r;
+            r.steps = ctl[CTL_STEP];
+            r.best = 0;
+            r.t_ns = global_ns() - *t0;
+            r.pad = 0;
+            rec[win] = r;
+        }
+    }
+}
+
 StepP make_step(const SolveDims &d, const DevCsr &J, Work &w)
 {
     StepP P;
@@ -128,14 +163,24 @@ StepP make_step(const SolveDims &d, const DevCsr &J, Work &w)
     P.hchunk = J.hchunk;
     P.chunk_row = J.chunk_row;
     P.part = (uint2 *)w.part;
+    P.hcount = w.hcount;
     P.nchunks = J.nchunks;
-    // several rows per warp: rows of a warp come in decreasing degree, so
-    // the walk to the warp's longest row wastes little
-    P.order = (J.skewed || d.tlr < 32) ? J.perm : nullptr;
+    P.order = nullptr;   // set per kernel (step_vl)
+    P.row0 = 0;
     P.c0r32 = J.c0r32;
     P.c0r64 = J.c0r64;
     P.n = d.n;
     P.W = d.W;
+    {
+        static int l2 = -1;
+        if (l2 < 0) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+        }
+        const double state = 2.0 * (double)d.n * d.Ap * prec_bytes(d.prec);
+        P.stream_state = state > 0.5 * (double)l2 ? 1 : 0;
+    }
     P.Ap = d.Ap;
     P.c0 = d.c0;
     return P;
@@ -176,8 +221,7 @@ cudaError_t launch_chunk(const SolveDims &d, const DevCsr &J, Work &w, cudaStrea
         e = step(d, J, P, d.fused ? K_FUSED : K_FC, i == d.period - 1, i, s);
         if (evs) cudaEventRecord(evs[2 * i + 1], s);
     }
-    // heavy-row partial counts: one more launch per step
-    *launches += d.period * ((J.unit && J.nchunks > 0) ? 2 : 1);
+    *launches += d.period;
     if (e != cudaSuccess) return e;
     WinP Q;
     Q.chg = w.chg;
@@ -199,6 +243,16 @@ cudaError_t launch_chunk(const SolveDims &d, const DevCsr &J, Work &w, cudaStrea
     e = launch(k_win_snap, dim3((unsigned)((d.n * d.W + 255) / 256)), dim3(256), 0, s, d.pdl, Q);
     *launches += 2;
     if (e != cudaSuccess || !d.trace) return e;
+    if (d.trace == 2) {
+        // batched: exact cuts per instance, best of each instance's agents
+        e = cudaMemsetAsync(w.eacc, 0, sizeof(unsigned long long) * J.ninst * d.Ap, s);
+        if (e == cudaSuccess) e = launch_cut_batch(d, J, w.Wp, w.eacc, s);
+        if (e != cudaSuccess) return e;
+        k_trace_batch<<<J.ninst, 64, 0, s>>>(w.eacc, d.Ap, J.iagents, J.iwsum, J.ninst, w.ctl, w.trace,
+                                             w.btrace, w.trace_t0, (int64_t)w.cap_trace);
+        *launches += 2;
+        return cudaGetLastError();
+    }
     // traced: exact cut of every agent's window spins, then the window's record
     e = launch_cut(d, J, w, w.Wp, s, launches);
     if (e != cudaSuccess) return e;

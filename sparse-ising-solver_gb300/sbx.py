@@ -40,7 +40,8 @@ class Params(C.Structure):
                 ("threshold", C.c_int32), ("precision", C.c_int32), ("seed", C.c_uint32),
                 ("kernel", C.c_int32), ("agents_per_block", C.c_int32), ("trace", C.c_int32),
                 ("flags", C.c_uint32), ("run_steps", C.c_int32), ("lane_agents", C.c_int32),
-                ("row_lanes", C.c_int32), ("block_threads", C.c_int32), ("target", C.c_double)]
+                ("row_lanes", C.c_int32), ("block_threads", C.c_int32), ("count_mode", C.c_int32),
+                ("target", C.c_double)]
 
 
 class Result(C.Structure):
@@ -50,7 +51,7 @@ class Result(C.Structure):
                 ("bifurcated", C.c_int64), ("valid", C.c_int64), ("best_agent", C.c_int32),
                 ("kernel_used", C.c_int32), ("agents_per_block", C.c_int32),
                 ("lane_agents", C.c_int32), ("row_lanes", C.c_int32), ("block_threads", C.c_int32),
-                ("kernel_ms", C.c_double), ("kernel_launches", C.c_int64),
+                ("count_mode", C.c_int32), ("kernel_ms", C.c_double), ("kernel_launches", C.c_int64),
                 ("gpu_launches", C.c_int64), ("time_to_target_us", C.c_double),
                 ("steps_to_target", C.c_int64)]
 
@@ -246,15 +247,17 @@ class Context:
         _check("sbx_solve", lib().sbx_solve(self._c, prob._p, C.byref(prm), C.byref(r), _p(vals)))
         return r.as_dict(), vals
 
-    def solve_batch(self, probs, agents, prm):
+    def solve_batch(self, probs, agents, prm, targets=None):
         n = len(probs)
         arr = (C.c_void_p * n)(*[p._p for p in probs])
         ag = np.ascontiguousarray(agents, np.int32)
+        tg = None if targets is None else np.ascontiguousarray(targets, np.float64)
         res = (Result * n)()
         vals = np.empty(int(ag.sum()))
         t = C.c_double()
         _check("sbx_solve_batch", lib().sbx_solve_batch(self._c, C.c_int32(n), arr, _p(ag),
-                                                        C.byref(prm), res, _p(vals), C.byref(t)))
+                                                        C.byref(prm), _p(tg), res, _p(vals),
+                                                        C.byref(t)))
         return [r.as_dict() for r in res], vals, t.value
 
     def state(self, n, agents):

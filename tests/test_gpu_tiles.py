@@ -29,7 +29,8 @@ def ctx():
 
 
 def _tiles(prec, Ap, heavy=False):
-    """The tiles a solve with Ap padded agents accepts (mirror of tile_ok)."""
+    """The tiles (agents per lane, lanes per row, threads per CTA) a solve
+    with Ap padded agents accepts (mirror of tile_ok)."""
     vm = {sbx.F64: 2, sbx.F32: 4, sbx.BF16: 8, sbx.F16: 8}[prec]
     out = []
     for v in (8, 4, 2, 1):
@@ -65,19 +66,22 @@ def _real_graph(n=203, p=0.05, seed=9):
 @pytest.mark.parametrize("weights", ["pm1", "real"])
 @pytest.mark.parametrize("agents", [64, 32, 128])
 def test_every_tile_gives_the_same_state(ctx, prec, weights, agents):
-    # 203 rows: not a multiple of 2, 4 or 8 rows per warp
+    # 203 rows: not a multiple of 2, 4 or 8 rows per warp; degrees up to ~20,
+    # so bit-plane counting splits rows over several lanes
     g = sbx.gen_er(203, 0.05, pm1=True, seed=7) if weights == "pm1" else _real_graph()
     prob = ctx.problem(g)
     Ap = (agents + 31) // 32 * 32
     tiles = _tiles(prec, Ap)
     assert any(lr < 32 for _, lr, _ in tiles) or prec == sbx.F64
+    modes = (1, 2) if weights == "pm1" else (1,)
     ref = None
-    for v, lr, bt in tiles:
+    for (v, lr, bt), cm in [(t, m) for t in tiles for m in modes]:
         r, cut = ctx.solve(prob, sbx.params(dt=0.4, steps=600, agents=agents, seed=11,
                                             precision=prec, update_window=1,
                                             kernel=sbx.KERNEL_STREAM, lane_agents=v,
-                                            row_lanes=lr, block_threads=bt))
-        assert (r["lane_agents"], r["row_lanes"], r["block_threads"]) == (v, lr, bt)
+                                            row_lanes=lr, block_threads=bt, count_mode=cm))
+        assert (r["lane_agents"], r["row_lanes"], r["block_threads"], r["count_mode"]) == \
+            (v, lr, bt, cm)
         x, y, s = ctx.state(g.n, agents)
         if ref is None:
             ref = (x, y, s, cut, r["steps_run"])
@@ -90,13 +94,14 @@ def test_every_tile_gives_the_same_state(ctx, prec, weights, agents):
 
 
 @pytest.mark.parametrize("fused", [1, 0])
-def test_fp64_rows_per_warp_tile_bitexact_with_oracle(ctx, oracle, fused):
+@pytest.mark.parametrize("count_mode", [1, 2])
+def test_fp64_rows_per_warp_tile_bitexact_with_oracle(ctx, oracle, fused, count_mode):
     g = sbx.gen_er(203, 0.05, pm1=True, seed=7)
     A, max_steps, dt, seed = 32, 2000, 0.3, 5
     prob = ctx.problem(g)
     ctx.solve(prob, sbx.params(dt=dt, steps=max_steps, run_steps=300, agents=A, fused=fused,
                                seed=seed, precision=sbx.F64, kernel=sbx.KERNEL_STREAM,
-                               lane_agents=2, row_lanes=16))
+                               lane_agents=2, row_lanes=16, count_mode=count_mode))
     x, y, s = ctx.state(g.n, A)
     og = oracle_graph(oracle, g)
     ox, oy = oracle_first_steps(oracle, og, A, seed, dt, max_steps, 300, fused)
@@ -128,8 +133,8 @@ def test_autotuned_tile_is_valid_and_changes_nothing(ctx, agents):
     assert tile in _tiles(sbx.BF16, agents)
     x, y, s = ctx.state(g.n, agents)
     r2, cut2 = ctx.solve(prob, sbx.params(flags=sbx.FLAG_NO_TUNE, **base))
-    assert (r2["lane_agents"], r2["row_lanes"], r2["block_threads"]) == \
-        ({64: 2, 1024: 8}[agents], 32, 256)
+    assert (r2["lane_agents"], r2["row_lanes"], r2["block_threads"], r2["count_mode"]) == \
+        ({64: 2, 1024: 8}[agents], 32, 256, 1)
     x2, y2, s2 = ctx.state(g.n, agents)
     np.testing.assert_array_equal(x, x2)
     np.testing.assert_array_equal(y, y2)
@@ -192,4 +197,48 @@ def test_trace_refused_where_not_built(ctx):
     assert e.value.rc == sbx.ERR_UNSUPPORTED
     with pytest.raises(sbx.SbxError) as e:
         ctx.solve_batch([prob], [64], sbx.params(steps=100, target=10.0))
-    assert e.value.rc == sbx.ERR_UNSUPPORTED
+    assert e.value.rc == sbx.ERR_ARG
+
+
+@pytest.mark.parametrize("prec", [sbx.BF16, sbx.F64])
+def test_batch_time_to_target_matches_single_traced_solves(ctx, prec):
+    # A batched instance runs exactly as alone from seed + i, so its first
+    # window reaching a target is the single traced solve's first window.
+    gs = [sbx.gen_er(300, 0.04, pm1=True, seed=1), sbx.gen_rgg(900, 8.0, seed=2),
+          sbx.gen_torus(20, 30, seed=3), sbx.gen_er(150, 0.1, pm1=False, seed=5)]
+    agents = [64, 64, 40, 64]
+    probs = [ctx.problem(g) for g in gs]
+    base = dict(dt=0.5, steps=1500, seed=100, precision=prec, kernel=sbx.KERNEL_STREAM)
+    res0, vals0, _ = ctx.solve_batch(probs, agents, sbx.params(**base))
+    # targets: a little under each instance's final best, and one out of reach
+    targets = [r["max"] - 2.0 for r in res0]
+    targets[2] = res0[2]["max"] + 1e6
+    res, vals, _ = ctx.solve_batch(probs, agents, sbx.params(**base), targets=targets)
+    np.testing.assert_array_equal(vals, vals0)       # the trace changes no result
+    for i, (p, a) in enumerate(zip(probs, agents)):
+        r1, _ = ctx.solve(p, sbx.params(agents=a, target=targets[i], **dict(base, seed=100 + i)))
+        assert res[i]["steps_to_target"] == r1["steps_to_target"]
+        if i == 2:
+            assert res[i]["steps_to_target"] == -1 and res[i]["time_to_target_us"] == -1
+        else:
+            assert 0 < res[i]["steps_to_target"] <= 1500 and res[i]["time_to_target_us"] > 0
+
+
+@pytest.mark.parametrize("agents", [32, 256])
+@pytest.mark.parametrize("count_mode", [1, 2])
+def test_dense_unit_rows_count_modes_bitexact_with_oracle(ctx, oracle, agents, count_mode):
+    # degrees ~100 (just under the heavy-row split at 127): every lane of a
+    # bit-plane group holds many neighbours and the planes fill up
+    g = sbx.gen_er(240, 0.42, pm1=True, seed=13)
+    deg = np.diff(g.rowptr)
+    assert deg.max() <= 127 and deg.mean() > 90
+    A, max_steps, dt, seed = agents, 2000, 0.2, 3
+    prob = ctx.problem(g)
+    # 200 steps: two windows of 100
+    ctx.solve(prob, sbx.params(dt=dt, steps=max_steps, run_steps=200, agents=A, fused=1, seed=seed,
+                               precision=sbx.F64, kernel=sbx.KERNEL_STREAM, count_mode=count_mode))
+    x, y, s = ctx.state(g.n, A)
+    og = oracle_graph(oracle, g)
+    ox, oy = oracle_first_steps(oracle, og, A, seed, dt, max_steps, 200, 1)
+    np.testing.assert_array_equal(x, ox)
+    np.testing.assert_array_equal(y, oy)
