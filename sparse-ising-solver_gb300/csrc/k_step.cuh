@@ -228,20 +228,52 @@ __device__ __forceinline__ void count_bits(const StepP &P, const uint32_t *Sq, i
     for (int i = 0; i < NP; i++) p[i] = 0;
     int32_t dmax = dw;
     if constexpr (LR < 32) dmax = __reduce_max_sync(FULL, dw);
-    for (int32_t cb = 0; cb < dmax; cb += LR) {
-        const int32_t idx = cb + sl;
-        const uint32_t mycw = idx < dw ? __ldg(&P.colw[e0 + idx]) : 0u;
-        const int m = min(LR, dmax - cb);
-        for (int k = 0; k < m; k += G) {
-            const int src = k + j;
-            const uint32_t cw = __shfl_sync(FULL, mycw, src, LR);
-            // past the row's end cw is 0: the load reads row 0, the term is dropped
-            const uint32_t w = __ldg(Sq + (size_t)(cw & 0x7fffffffu) * (size_t)P.W);
-            uint32_t c = (cb + src < dw) ? (w ^ (uint32_t)((int32_t)cw >> 31)) : 0u;
+    // Blocks of 32 neighbours: the row's lanes load 32/LR column words each,
+    // every lane issues its 32/G sign-word loads, then adds them -- one
+    // memory latency per block.  Sub-blocks past the longest row of the
+    // warp are skipped (warp-uniform).
+    constexpr int T = 32 / LR;     // column words per lane per block
+    constexpr int KPL = LR / G;    // neighbours per lane per column word
+    for (int32_t cb = 0; cb < dmax; cb += 32) {
+        uint32_t mycw[T];
 #pragma unroll
-            for (int i = 0; i < BL; i++) {
-                const uint32_t t = p[i] & c;
-                p[i] ^= c;
+        for (int t = 0; t < T; t++) {
+            const int32_t idx = cb + t * LR + sl;
+            mycw[t] = idx < dw ? __ldg(&P.colw[e0 + idx]) : 0u;
+        }
+        uint32_t w[T * KPL];
+#pragma unroll
+        for (int t = 0; t < T; t++) {
+#pragma unroll
+            for (int kk = 0; kk < KPL; kk++) {
+                const int src = kk * G + j;
+                const uint32_t cw = __shfl_sync(FULL, mycw[t], src, LR);
+                w[t * KPL + kk] = 0u;
+                if (cb + t * LR < dmax) {
+                    // past the row's end cw is 0: row 0 is read, the term dropped
+                    const uint32_t word = __ldg(Sq + (size_t)(cw & 0x7fffffffu) * (size_t)P.W);
+                    w[t * KPL + kk] = (cb + t * LR + src < dw) ? (word ^ (uint32_t)((int32_t)cw >> 31)) : 0u;
+                }
+            }
+        }
+        // pairs of words through a full adder into plane 0, the carry
+        // rippling up the planes
+#pragma unroll
+        for (int i = 0; i < T * KPL; i += 2) {
+            if (cb + (i / KPL) * LR >= dmax) break;   // warp-uniform
+            uint32_t c;
+            if (i + 1 < T * KPL) {
+                const uint32_t a = p[0], b = w[i], e = w[i + 1];
+                p[0] = a ^ b ^ e;
+                c = (a & b) | (e & (a ^ b));
+            } else {
+                c = p[0] & w[i];
+                p[0] ^= w[i];
+            }
+#pragma unroll
+            for (int k = 1; k < BL; k++) {
+                const uint32_t t = p[k] & c;
+                p[k] ^= c;
                 c = t;
             }
         }
@@ -351,8 +383,11 @@ __device__ __forceinline__ void sb_update(double (&x)[V], double (&y)[V], const 
 // the warp completing a row's last chunk (a per-row counter, re-armed by that
 // warp) sums them and updates the row.  The other rows follow, in decreasing
 // degree when P.order is set.
+// Resident CTAs per SM asked of the register allocator (measured on GB300):
+// 6 for heavy-row kernels, 4 for bit-plane counting (its loads in flight
+// need registers), 5 otherwise.
 template <class T, int V, int KIND, bool WIN, int WM, bool BIG, int LR, int CM>
-__global__ void __launch_bounds__(256, BIG ? 6 : 1) k_row(const StepP P, const int offset)
+__global__ void __launch_bounds__(256, BIG ? 6 : (CM ? 4 : 5)) k_row(const StepP P, const int offset)
 {
     static_assert(LR == 32 || !BIG, "heavy rows are counted by whole warps");
     static_assert(LR * V >= 32, "a sign word belongs to one row's lanes");
