@@ -263,6 +263,7 @@ def main():
 
     import torch
     import sbx
+    import replicas
 
     torch.cuda.set_device(local)
     dist = None
@@ -319,13 +320,8 @@ def main():
                 launches += res["gpu_launches"]
             torch.cuda.synchronize()
         ms = sum(a.elapsed_time(b) for a, b in evs)
-        if dist is not None:
-            t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-            u = torch.tensor([units], device="cuda", dtype=torch.float64)
-            dist.all_reduce(u)
-            units = float(u.item())
+        # replicas: the slowest rank's time, all ranks' work
+        ms, units = replicas.reduce_timing(ms, units, device="cuda")
         return units / (ms / 1000.0), ms / k, res, clk.summary(), launches // max(k, 1)
 
     main_prec = wl["precision"]
@@ -459,7 +455,11 @@ def run_batch(args, wl, rank, world, local):
     import numpy as np
     import torch
     import sbx
+    import replicas
     torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     ctx = sbx.Context(local)
@@ -490,7 +490,9 @@ def run_batch(args, wl, rank, world, local):
         torch.cuda.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
     steps_run = res[0]["steps_run"]
-    value = units_per * steps_run / (ms / 1000.0)
+    # replicas: the slowest rank's time, all ranks' work
+    ms, units_all = replicas.reduce_timing(ms, units_per * steps_run, device="cuda")
+    value = units_all / (ms / 1000.0)
     best_b = np.array([r["max"] for r in res])
     launches = res[0]["gpu_launches"]
     # e2e: upload every instance from host buffers, solve, read back
@@ -567,6 +569,9 @@ def run_batch(args, wl, rank, world, local):
         }
         print(json.dumps(line), flush=True)
     ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
 
 
 if __name__ == "__main__":
