@@ -16,6 +16,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -86,8 +87,29 @@ struct Entry {
     double v;
 };
 
+// Host threads for the loaders: all hardware threads, at most 64.
+int host_threads()
+{
+    const unsigned h = std::thread::hardware_concurrency();
+    return (int)std::max(1u, std::min(h, 64u));
+}
+
+// Run f(t, T) on T threads (t = 0..T-1); T = 1 runs inline.
+template <class F> void parallel(int T, F f)
+{
+    if (T <= 1) {
+        f(0, 1);
+        return;
+    }
+    std::vector<std::thread> th;
+    th.reserve((size_t)T);
+    for (int t = 0; t < T; t++) th.emplace_back(f, t, T);
+    for (auto &x : th) x.join();
+}
+
 // construct_csr with every row kept: counting sort by row, then (col, value)
-// within the row, which is the order of std::sort on the tuples.
+// within the row, which is the order of std::sort on the tuples
+// (src/csr.cpp:157-192).  The rows are sorted by host threads in parallel.
 void to_csr(int64_t n, std::vector<Entry> &t, int32_t *rowptr, int32_t *col, double *val)
 {
     std::vector<int64_t> cnt((size_t)n + 1, 0);
@@ -96,15 +118,95 @@ void to_csr(int64_t n, std::vector<Entry> &t, int32_t *rowptr, int32_t *col, dou
     std::vector<Entry> s(t.size());
     std::vector<int64_t> at(cnt.begin(), cnt.end() - 1);
     for (auto &e : t) s[(size_t)at[e.r]++] = e;
-    for (int64_t i = 0; i < n; i++)
-        std::sort(s.begin() + cnt[i], s.begin() + cnt[i + 1], [](const Entry &a, const Entry &b) {
-            return a.c != b.c ? a.c < b.c : a.v < b.v;
-        });
+    const int T = t.size() > (1u << 20) ? host_threads() : 1;
+    parallel(T, [&](int k, int K) {
+        const int64_t r0 = n * k / K, r1 = n * (k + 1) / K;
+        for (int64_t i = r0; i < r1; i++)
+            std::sort(s.begin() + cnt[i], s.begin() + cnt[i + 1], [](const Entry &a, const Entry &b) {
+                return a.c != b.c ? a.c < b.c : a.v < b.v;
+            });
+        for (int64_t k2 = cnt[r0]; k2 < cnt[r1]; k2++) {
+            col[k2] = s[(size_t)k2].c;
+            val[k2] = s[(size_t)k2].v;
+        }
+    });
     for (int64_t i = 0; i <= n; i++) rowptr[i] = (int32_t)cnt[i];
-    for (size_t k = 0; k < s.size(); k++) {
-        col[k] = s[k].c;
-        val[k] = s[k].v;
+}
+
+// The L entries "r c [v]" of an .mtx body from text position pos, the
+// diagonal dropped, in file order.  Large bodies are cut at newlines into
+// one piece per host thread and parsed in parallel; a piece that does not
+// end on an entry boundary (an entry spread over lines) sends the whole body
+// to the sequential parse, which reads tokens like istream's operator>>.
+// Returns SBX_OK, SBX_ERR_FORMAT (short or malformed body, index out of range).
+int parse_entries(Text &f, long long M, long long L, bool pattern, std::vector<Entry> &out)
+{
+    const size_t body = f.pos, end = f.size();
+    const int T = (end - body) > (8u << 20) ? host_threads() : 1;
+    if (T > 1) {
+        std::vector<size_t> cut((size_t)T + 1);
+        cut[0] = body;
+        cut[(size_t)T] = end;
+        for (int t = 1; t < T; t++) {
+            size_t c = body + (end - body) * (size_t)t / (size_t)T;
+            while (c < end && f.buf[c] != '\n') c++;
+            cut[(size_t)t] = std::max(c, cut[(size_t)t - 1]);
+        }
+        std::vector<std::vector<Entry>> part((size_t)T);
+        std::vector<long long> nread((size_t)T, 0);
+        std::vector<int> bad((size_t)T, 0);
+        parallel(T, [&](int t, int) {
+            Text g;   // a view of the piece: parse with the same tokenizer
+            g.buf.assign(f.buf.begin() + (long)cut[(size_t)t], f.buf.begin() + (long)cut[(size_t)t + 1]);
+            g.buf.push_back(0);
+            auto &v = part[(size_t)t];
+            for (;;) {
+                long long r, c;
+                double d = 1;
+                const size_t before = g.pos;
+                if (!g.integer(r)) {
+                    // only whitespace may remain
+                    while (g.pos < g.size() && Text::ws(g.buf[g.pos])) g.pos++;
+                    if (g.pos < g.size()) bad[(size_t)t] = 1;
+                    break;
+                }
+                if (!g.integer(c) || (!pattern && !g.real(d))) {
+                    bad[(size_t)t] = 1;   // entry split across pieces or malformed
+                    g.pos = before;
+                    break;
+                }
+                nread[(size_t)t]++;
+                v.push_back({(int32_t)(r < 1 || r > M ? -1 : r - 1), (int32_t)(c < 1 || c > M ? -1 : c - 1), d});
+            }
+        });
+        bool ok = true;
+        for (int t = 0; t < T; t++) ok = ok && !bad[(size_t)t];
+        if (ok) {
+            long long total = 0;
+            for (int t = 0; t < T; t++) total += nread[(size_t)t];
+            if (total < L) return SBX_ERR_FORMAT;
+            out.clear();
+            out.reserve((size_t)L);
+            long long taken = 0;
+            for (int t = 0; t < T && taken < L; t++)
+                for (const Entry &e : part[(size_t)t]) {
+                    if (taken == L) break;
+                    taken++;
+                    if (e.r < 0 || e.c < 0) return SBX_ERR_FORMAT;
+                    if (e.r != e.c) out.push_back(e);
+                }
+            return SBX_OK;
+        }
     }
+    out.clear();
+    for (long long l = 0; l < L; l++) {
+        long long r, c;
+        double d = 1;
+        if (!f.integer(r) || !f.integer(c) || (!pattern && !f.real(d))) return SBX_ERR_FORMAT;
+        if (r < 1 || r > M || c < 1 || c > M) return SBX_ERR_FORMAT;
+        if (r != c) out.push_back({(int32_t)(r - 1), (int32_t)(c - 1), d});
+    }
+    return SBX_OK;
 }
 
 // splitmix64: the seeded generator of the synthetic instances.
@@ -169,17 +271,11 @@ int sbx_load_mtx(const char *path, int64_t *n_out, int64_t *nnz_out, int32_t *ro
         return SBX_ERR_FORMAT;
     std::vector<Entry> t;
     t.reserve((size_t)L * (symmetric ? 2 : 1));
+    const int prc = parse_entries(f, M, L, pattern, t);
+    if (prc) return prc;
+    // W in file order, as the reference accumulates it (src/csr.cpp:69)
     double sum = 0;
-    for (long long l = 0; l < L; l++) {
-        long long r, c;
-        double d = 1;
-        if (!f.integer(r) || !f.integer(c) || (!pattern && !f.real(d))) return SBX_ERR_FORMAT;
-        if (r < 1 || r > M || c < 1 || c > M) return SBX_ERR_FORMAT;
-        if (r != c) {
-            t.push_back({(int32_t)(r - 1), (int32_t)(c - 1), d});
-            sum += d;
-        }
-    }
+    for (const Entry &e : t) sum += e.v;
     if (symmetric) {
         const size_t m0 = t.size();
         for (size_t i = 0; i < m0; i++) t.push_back({t[i].c, t[i].r, t[i].v});

@@ -158,3 +158,56 @@ def test_cli_usage_and_errors(tmp_path):
     r = subprocess.run([prog, "1", str(tmp_path / "missing.mtx"), str(tmp_path / "o.csv")],
                        capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "cannot open" in r.stderr
+
+
+def _big_mtx(path, n=200000, m=1200000, seed=4, real=True, split_one=False):
+    rng = np.random.default_rng(seed)
+    r = rng.integers(1, n + 1, m)
+    c = rng.integers(1, n + 1, m)
+    c[::97] = r[::97]                      # some diagonal entries, dropped on load
+    v = np.round(rng.normal(0, 1, m), 4)
+    with open(path, "w") as f:
+        f.write("%%MatrixMarket matrix coordinate real symmetric\n%% generated\n")
+        f.write("%d %d %d\n" % (n, n, m))
+        lines = ["%d %d %.4f" % t for t in zip(r, c, v)] if real else ["%d %d" % t for t in zip(r, c)]
+        if split_one:
+            k = len(lines) // 2
+            a, b, w = lines[k].split(" ")
+            lines[k] = a + "\n" + b + " " + w   # one entry over two lines
+        f.write("\n".join(lines) + "\n")
+
+
+@pytest.mark.parametrize("split_one", [False, True])
+def test_large_mtx_parallel_parse_matches_oracle(tmp_path, oracle, split_one):
+    # bodies over 8 MB are parsed by every host thread; an entry spread over
+    # two lines sends the file back to the sequential parse
+    path = str(tmp_path / "big.mtx")
+    _big_mtx(path, split_one=split_one)
+    assert os.path.getsize(path) > 8 << 20
+    g = sbx.load_mtx(path)
+    ref = oracle.mtx_load(path)
+    assert g.n == ref.n
+    np.testing.assert_array_equal(g.rowptr, ref.rowptr)
+    np.testing.assert_array_equal(g.col, ref.col)
+    np.testing.assert_array_equal(g.val, ref.val)
+    assert g.wsum == ref.wsum
+
+
+def test_large_mtx_errors(tmp_path):
+    path = str(tmp_path / "bad.mtx")
+    _big_mtx(path)
+    with open(path) as f:
+        text = f.read()
+    k = len(text) * 3 // 4
+    k = text.index("\n", k) + 1
+    with open(path, "w") as f:
+        f.write(text[:k] + "12 x 0.5\n" + text[k:])      # a malformed entry in a late piece
+    n = C.c_int64()
+    nnz = C.c_int64()
+    w = C.c_double()
+    rc = sbx.lib().sbx_load_mtx(path.encode(), C.byref(n), C.byref(nnz), None, None, None, C.byref(w))
+    assert rc == -5
+    with open(path, "w") as f:
+        f.write(text[:len(text) // 2])                   # fewer entries than announced
+    rc = sbx.lib().sbx_load_mtx(path.encode(), C.byref(n), C.byref(nnz), None, None, None, C.byref(w))
+    assert rc == -5
