@@ -36,7 +36,6 @@ struct sbx_problem {
     bool tsp = false;
     DevCsr J;
     DevTsp T;
-    mutable std::map<std::string, Tile> tiles;   // autotuned tiles by precision/agents/mode
 };
 
 // A class of batched instances sharing one padded agent count, packed into
@@ -50,7 +49,6 @@ struct BatchClass {
     int32_t Ap = 0;
     DevCsr J;
     double dt = -1;                       // dt of the uploaded per-row c0
-    std::map<std::string, Tile> tiles;
 };
 
 struct sbx_ctx {
@@ -73,6 +71,9 @@ struct sbx_ctx {
     std::vector<BatchClass> batch;      // packed classes of the last batch
     std::string batch_key;
     std::vector<TraceRec> trace;        // per-window records of the last traced solve
+    // autotuned tiles by matrix shape (rows, entries, degrees, weight kind),
+    // precision, agents and mode: a problem uploaded again reuses its tile
+    std::map<std::string, Tile> tiles;
 };
 
 namespace {
@@ -427,8 +428,7 @@ int default_v(const SolveDims &d)
 // come from the problem's cache or from timing every candidate tile over a
 // few plain steps on the live state (*timed then asks the caller to set the
 // initial state again).  Every tile computes the same results.
-int pick_tile(sbx_ctx *ctx, std::map<std::string, Tile> &cache, SolveDims &d, const DevCsr &J,
-              const sbx_params *pr, bool *timed)
+int pick_tile(sbx_ctx *ctx, SolveDims &d, const DevCsr &J, const sbx_params *pr, bool *timed)
 {
     *timed = false;
     const bool big = J.unit && J.nchunks > 0;
@@ -461,8 +461,11 @@ int pick_tile(sbx_ctx *ctx, std::map<std::string, Tile> &cache, SolveDims &d, co
             if (t.v == default_v(d) && t.lr == 32 && t.bt == 256 && t.cm == 0) apply(t);
         return SBX_OK;
     }
-    char key[96];
-    snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d/%d", d.prec, d.Ap, d.fused, fv, flr, fbt, fcm);
+    char key[192];
+    snprintf(key, sizeof key, "%lld/%lld/%d/%d/%lld/%d%d%d/%d/%d/%d/%d/%d/%d/%d", (long long)J.n,
+             (long long)J.nnz, J.max_deg, J.nchunks, (long long)J.nheavy, (int)J.unit, (int)J.skewed,
+             (int)(J.c0r32 != nullptr), d.prec, d.Ap, d.fused, fv, flr, fbt, fcm);
+    auto &cache = ctx->tiles;
     auto it = cache.find(key);
     if (it != cache.end()) {
         apply(it->second);
@@ -635,7 +638,7 @@ int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_r
         return fail(ctx, SBX_ERR_UNSUPPORTED, "resident kernel: shape does not fit on chip (or FP64)");
     if (!ka) {
         bool timed = false;
-        if ((rc = pick_tile(ctx, p->tiles, d, p->J, pr, &timed))) return rc;
+        if ((rc = pick_tile(ctx, d, p->J, pr, &timed))) return rc;
         if (timed && (rc = init_state(ctx, d, pr->seed, false))) return rc;
     }
     int launches = 0, hot = 0;
@@ -775,10 +778,14 @@ int solve_tsp(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
         CK(cudaMemcpyAsync(w.ctl, c2, sizeof c2, cudaMemcpyHostToDevice, s));
     }
     CK(cudaEventRecord(ctx->ev1, s));
-    std::vector<int32_t> tours((size_t)d.A * t.N), valid((size_t)d.A);
+    // tour lengths on the device (src/ising_tsp.cu:272-287, FP64 in tour order)
+    CK(launch_tsp_lengths(t, w.tours, w.valid, d.A, w.cut, s));
+    launches++;
+    std::vector<int32_t> valid((size_t)d.A);
+    std::vector<double> lens((size_t)d.A);
     std::vector<uint8_t> bif((size_t)d.A);
     int32_t ctl[CTL_N];
-    CK(cudaMemcpyAsync(tours.data(), w.tours, tours.size() * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(lens.data(), w.cut, lens.size() * 8, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(valid.data(), w.valid, valid.size() * 4, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(bif.data(), w.bif, d.A, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(ctl, w.ctl, sizeof ctl, cudaMemcpyDeviceToHost, s));
@@ -796,12 +803,7 @@ int solve_tsp(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
     for (int32_t a = 0; a < d.A; a++) {
         double len = NAN;
         if (valid[a] > 0) {
-            len = 0.0;
-            for (int i = 0; i < N; i++) {
-                const int c1 = std::min(tours[(size_t)a * N + i], tours[(size_t)a * N + (i + 1) % N]);
-                const int c2 = std::max(tours[(size_t)a * N + i], tours[(size_t)a * N + (i + 1) % N]);
-                len += t.packed[(size_t)(c2 + c1 * N - (c1 + 2) * (c1 + 1) / 2)];
-            }
+            len = lens[(size_t)a];
             all.push_back(len);
             total_len += len;
             if (len < mn) {
@@ -831,6 +833,9 @@ int solve_tsp(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
     res->kernel_used = ka ? SBX_KERNEL_RESIDENT : SBX_KERNEL_STREAM;
     res->agents_per_block = ka;
     res->kernel_launches = hot;
+    // SBX_FLAG_PROFILE: the SB loop's kernels (the whole solve is one
+    // resident launch, or the streaming steps and windows)
+    res->kernel_ms = (pr->flags & SBX_FLAG_PROFILE) ? ms : 0.0;
     res->gpu_launches = launches + 1;
     ctx->have = true;
     ctx->last_tsp = true;
@@ -1005,7 +1010,7 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
         if ((rc = init_instances(ctx, d, inst, false))) return rc;
         if (nchunks) {
             bool timed = false;
-            if ((rc = pick_tile(ctx, c.tiles, d, c.J, pr, &timed))) return rc;
+            if ((rc = pick_tile(ctx, d, c.J, pr, &timed))) return rc;
             if (timed && (rc = init_instances(ctx, d, inst, false))) return rc;
         }
         int launches = 0;
@@ -1269,6 +1274,14 @@ int sbx_problem_tsp(sbx_ctx *ctx, int32_t N, const double *packed, double A, dou
     cudaError_t e = cudaMalloc(&t.D, sizeof(float) * N * N);
     if (e == cudaSuccess) e = cudaMalloc(&t.I2, sizeof(float) * N);
     if (e == cudaSuccess) e = cudaMalloc(&t.I2d, sizeof(double) * N);
+    if (e == cudaSuccess) e = cudaMalloc(&t.Dd, sizeof(double) * N * N);
+    if (e == cudaSuccess) {
+        std::vector<double> Dd((size_t)N * N, 0.0);
+        for (int k = 0; k < N; k++)
+            for (int l = 0; l < N; l++)
+                if (k != l) Dd[(size_t)k * N + l] = packed[pidx(std::min(k, l), std::max(k, l))];
+        e = cudaMemcpy(t.Dd, Dd.data(), sizeof(double) * N * N, cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) e = cudaMemcpy(t.D, D.data(), sizeof(float) * N * N, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(t.I2, I2f.data(), sizeof(float) * N, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(t.I2d, t.I2h.data(), sizeof(double) * N, cudaMemcpyHostToDevice);
@@ -1306,6 +1319,7 @@ int sbx_problem_tsp(sbx_ctx *ctx, int32_t N, const double *packed, double A, dou
         cudaFree(t.D);
         cudaFree(t.I2);
         cudaFree(t.I2d);
+        cudaFree(t.Dd);
         free_csr(t.qubo);
         delete p;
         return rc;
@@ -1338,6 +1352,7 @@ int sbx_problem_destroy(sbx_problem *p)
     cudaFree(p->T.D);
     cudaFree(p->T.I2);
     cudaFree(p->T.I2d);
+    cudaFree(p->T.Dd);
     delete p;
     return SBX_OK;
 }

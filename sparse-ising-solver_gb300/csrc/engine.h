@@ -40,7 +40,7 @@ struct DevCsr {
     bool skewed = false;     // max degree > 8x mean: the step kernel visits rows in perm order
     int64_t nheavy = 0;      // heavy rows: the first nheavy entries of perm
     // Heavy rows (unit weights, degree > kHeavy) are split into chunks of
-    // kHeavy neighbours whose partial counts a separate kernel computes.
+    // kHeavy neighbours, each counted by its own work item of the step kernel.
     int32_t *hchunk = nullptr;    // per row: first chunk of a heavy row, else -1
     int32_t *chunk_row = nullptr; // per chunk: its row
     int32_t nchunks = 0;
@@ -164,6 +164,7 @@ struct DevTsp {
     float *D = nullptr;                   // device N x N distances (float)
     float *I2 = nullptr;                  // device per-city linear field (float)
     double *I2d = nullptr;                // the same in FP64
+    double *Dd = nullptr;                 // device N x N distances (FP64, exact)
     DevCsr qubo;                          // the QUBO as CSR (streaming path)
 };
 int tsp_pick_ka(const SolveDims &d, const DevTsp &t, int requested);
@@ -171,5 +172,8 @@ cudaError_t launch_tsp_resident(const SolveDims &d, const DevTsp &t, Work &w, in
                                 cudaStream_t s);
 cudaError_t launch_tsp_stream(const SolveDims &d, const DevTsp &t, Work &w, cudaStream_t s,
                               int *launches);
+// Tour length of every agent holding a valid tour (NaN otherwise) into len[A].
+cudaError_t launch_tsp_lengths(const DevTsp &t, const int32_t *tours, const int32_t *valid, int32_t A,
+                               double *len, cudaStream_t s);
 
 }  // namespace sbx

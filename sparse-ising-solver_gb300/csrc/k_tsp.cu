@@ -525,4 +525,38 @@ cudaError_t launch_tsp_stream(const SolveDims &d, const DevTsp &t, Work &w, cuda
     }
 }
 
+namespace {
+
+// Length of agent a's tour: the packed distance of every consecutive pair,
+// the last city back to the first, summed in tour order in FP64 (src/ising_tsp.cu:272-287).
+__global__ void __launch_bounds__(128) k_tsp_lengths(const int32_t *__restrict__ tours,
+                                                     const int32_t *__restrict__ valid,
+                                                     const double *__restrict__ Dd, int32_t N, int32_t A,
+                                                     double *len)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= A) return;
+    if (valid[a] <= 0) {
+        len[a] = __longlong_as_double(0x7ff8000000000000LL);   // NaN: no valid tour
+        return;
+    }
+    const int32_t *t = tours + (int64_t)a * N;
+    double s = 0.0;
+    for (int i = 0; i < N; i++) {
+        const int c1 = t[i], c2 = t[i + 1 < N ? i + 1 : 0];
+        s = __dadd_rn(s, Dd[(int64_t)c1 * N + c2]);
+    }
+    len[a] = s;
+}
+
+}  // namespace
+
+cudaError_t launch_tsp_lengths(const DevTsp &t, const int32_t *tours, const int32_t *valid, int32_t A,
+                               double *len, cudaStream_t s)
+{
+    if (A <= 0) return cudaSuccess;
+    k_tsp_lengths<<<(A + 127) / 128, 128, 0, s>>>(tours, valid, t.Dd, t.N, A, len);
+    return cudaGetLastError();
+}
+
 }  // namespace sbx

@@ -139,9 +139,14 @@ def test_autotuned_tile_is_valid_and_changes_nothing(ctx, agents):
     np.testing.assert_array_equal(x, x2)
     np.testing.assert_array_equal(y, y2)
     np.testing.assert_array_equal(cut, cut2)
-    # the tuned tile is cached per problem: the same tile again
+    # the tuned tile is cached by matrix shape: the same tile again, also for a
+    # fresh upload of the same graph
     r3, _ = ctx.solve(prob, sbx.params(**base))
     assert (r3["lane_agents"], r3["row_lanes"], r3["block_threads"]) == tile
+    prob2 = ctx.problem(g)
+    r4, cut4 = ctx.solve(prob2, sbx.params(**base))
+    assert (r4["lane_agents"], r4["row_lanes"], r4["block_threads"]) == tile
+    np.testing.assert_array_equal(cut4, cut)
 
 
 def test_trace_and_time_to_target(ctx, oracle):
