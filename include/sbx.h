@@ -41,8 +41,11 @@ extern "C" {
 
 /* agent-state storage precision (arithmetic of the force is exact) */
 enum { SBX_F32 = 0, SBX_BF16 = 1, SBX_F16 = 2, SBX_F64 = 3 };
-/* kernel family: chosen by shape (AUTO) or forced */
-enum { SBX_KERNEL_AUTO = 0, SBX_KERNEL_STREAM = 1, SBX_KERNEL_RESIDENT = 2 };
+/* kernel family: chosen by shape (AUTO) or forced.  RESIDENT keeps a CTA's
+ * agents in shared memory; RESIDENT_SPLIT (MaxCut, fused, 16-bit state) keeps
+ * 8 agents per CTA split between registers and shared memory, for graphs too
+ * large for the former. */
+enum { SBX_KERNEL_AUTO = 0, SBX_KERNEL_STREAM = 1, SBX_KERNEL_RESIDENT = 2, SBX_KERNEL_RESIDENT_SPLIT = 3 };
 /* TSP distance kinds, src/kernels.cu:404-442 */
 enum { SBX_DIST_EUC_2D = 0, SBX_DIST_GEO = 1, SBX_DIST_EUC_2D_FLOAT = 2 };
 /* sbx_params.flags */

@@ -137,6 +137,12 @@ void free_csr(DevCsr &J)
     cudaFree(J.rinst);
     cudaFree(J.iagents);
     cudaFree(J.iwsum);
+    cudaFree(J.rs_rowptr);
+    cudaFree(J.rs_colw);
+    cudaFree(J.rs_valf);
+    J.rs_rowptr = nullptr;
+    J.rs_colw = nullptr;
+    J.rs_valf = nullptr;
     J.iagents = nullptr;
     J.iwsum = nullptr;
     J.ninst = 0;
@@ -202,6 +208,7 @@ int upload_csr(sbx_ctx *ctx, DevCsr &J, int64_t n, int64_t nnz, const int32_t *r
     J.hval.assign(val, val + nnz);
     J.hrowptr.assign(rowptr, rowptr + n + 1);
     J.hcol.assign(col, col + nnz);
+    J.hperm = perm;
     CK(cudaMalloc(&J.rowptr, sizeof(int32_t) * (n + 1)));
     CK(cudaMalloc(&J.colw, sizeof(uint32_t) * std::max<int64_t>(nnz, 1)));
     CK(cudaMalloc(&J.vald, sizeof(double) * std::max<int64_t>(nnz, 1)));
@@ -599,6 +606,8 @@ int run_stream(sbx_ctx *ctx, const void *key_obj, const SolveDims &d, const DevC
     return SBX_OK;
 }
 
+int ensure_rs_csr(sbx_ctx *ctx, DevCsr &J);
+
 int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_result *res,
                  double *agent_values)
 {
@@ -632,28 +641,40 @@ int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_r
     if ((rc = upload_coef(ctx, d, total))) return rc;
     if ((rc = init_state(ctx, d, pr->seed, false))) return rc;
 
-    int ka = 0;
-    if (pr->kernel != SBX_KERNEL_STREAM && !d.trace) ka = resident_pick_ka(d, p->J, pr->agents_per_block);
+    // on-chip kernels first: shared-memory resident, then register + shared
+    int ka = 0, rs = 0;
+    if ((pr->kernel == SBX_KERNEL_AUTO || pr->kernel == SBX_KERNEL_RESIDENT) && !d.trace)
+        ka = resident_pick_ka(d, p->J, pr->agents_per_block);
+    if ((pr->kernel == SBX_KERNEL_AUTO || pr->kernel == SBX_KERNEL_RESIDENT_SPLIT) && !d.trace && !ka &&
+        !pr->agents_per_block)
+        rs = resident_rs_pick(d, p->J, pr->kernel == SBX_KERNEL_RESIDENT_SPLIT);
     if (pr->kernel == SBX_KERNEL_RESIDENT && !ka)
         return fail(ctx, SBX_ERR_UNSUPPORTED, "resident kernel: shape does not fit on chip (or FP64)");
-    if (!ka) {
+    if (pr->kernel == SBX_KERNEL_RESIDENT_SPLIT && !rs)
+        return fail(ctx, SBX_ERR_UNSUPPORTED,
+                    "split resident kernel: 16-bit fused state, degree <= 127 and fitting on chip only");
+    if (rs && (rc = ensure_rs_csr(ctx, const_cast<DevCsr &>(p->J)))) return rc;
+    if (!ka && !rs) {
         bool timed = false;
         if ((rc = pick_tile(ctx, d, p->J, pr, &timed))) return rc;
         if (timed && (rc = init_state(ctx, d, pr->seed, false))) return rc;
     }
     int launches = 0, hot = 0;
     CK(cudaEventRecord(ctx->ev0, s));
-    if (ka) {
+    auto resident = [&](int32_t step0, int32_t nsteps, bool first) {
+        return ka ? launch_resident(d, p->J, ctx->w, ka, step0, nsteps, first, s)
+                  : launch_resident_rs(d, p->J, ctx->w, rs, step0, nsteps, first, s);
+    };
+    if (ka || rs) {
         if (d.uw) {
             for (int64_t c = 0; c < std::max<int64_t>(nchunks, 1); c++) {
-                CK(launch_resident(d, p->J, ctx->w, ka, (int32_t)(c * d.period),
-                                   nchunks ? d.period : 0, c == 0, s));
+                CK(resident((int32_t)(c * d.period), nchunks ? d.period : 0, c == 0));
                 launches++;
                 hot++;
                 if (poll_stop(ctx, c, false)) break;
             }
         } else {
-            CK(launch_resident(d, p->J, ctx->w, ka, 0, (int32_t)total, true, s));
+            CK(resident(0, (int32_t)total, true));
             launches++;
             hot++;
         }
@@ -681,16 +702,16 @@ int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_r
     res->steps_run = ctl[CTL_STEP];
     res->windows_run = ctl[CTL_WINDOWS];
     for (uint8_t b : bif) res->bifurcated += b;
-    res->kernel_used = ka ? SBX_KERNEL_RESIDENT : SBX_KERNEL_STREAM;
-    res->agents_per_block = ka;
-    if (!ka) {
+    res->kernel_used = ka ? SBX_KERNEL_RESIDENT : rs ? SBX_KERNEL_RESIDENT_SPLIT : SBX_KERNEL_STREAM;
+    res->agents_per_block = ka ? ka : rs ? 8 : 0;
+    if (!ka && !rs) {
         res->lane_agents = d.tv ? d.tv : default_v(d);
         res->row_lanes = d.tlr;
         res->block_threads = d.tbt;
         res->count_mode = d.tcm + 1;
     }
     if ((rc = read_trace(ctx, d, ctl[CTL_TRACED], pr->target, res))) return rc;
-    if (ka) {
+    if (ka || rs) {
         res->kernel_launches = hot;
         res->kernel_ms = profile ? ms : 0;
     } else {
@@ -885,6 +906,36 @@ int build_class(sbx_ctx *ctx, BatchClass &c)
     CK(cudaMalloc(&c.J.iwsum, sizeof(double) * c.J.ninst));
     CK(cudaMemcpy(c.J.iagents, c.agents.data(), sizeof(int32_t) * c.J.ninst, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c.J.iwsum, c.wsum.data(), sizeof(double) * c.J.ninst, cudaMemcpyHostToDevice));
+    return SBX_OK;
+}
+
+// The matrix in perm order for the register + shared resident kernel: row s
+// is row perm[s], its columns renamed to their slots, entries in the original
+// order within the row (the FP32 sums of real weights keep their order).
+int ensure_rs_csr(sbx_ctx *ctx, DevCsr &J)
+{
+    if (J.rs_rowptr) return SBX_OK;
+    const int64_t n = J.n;
+    std::vector<int32_t> inv((size_t)n), rp((size_t)n + 1, 0);
+    for (int64_t s = 0; s < n; s++) inv[(size_t)J.hperm[(size_t)s]] = (int32_t)s;
+    std::vector<uint32_t> cw((size_t)std::max<int64_t>(J.nnz, 1));
+    std::vector<float> vf((size_t)std::max<int64_t>(J.nnz, 1));
+    int64_t e = 0;
+    for (int64_t s = 0; s < n; s++) {
+        const int32_t r = J.hperm[(size_t)s];
+        for (int32_t k = J.hrowptr[(size_t)r]; k < J.hrowptr[(size_t)r + 1]; k++, e++) {
+            const double v = J.hval[(size_t)k];
+            cw[(size_t)e] = (uint32_t)inv[(size_t)J.hcol[(size_t)k]] | ((J.unit && v < 0) ? 0x80000000u : 0u);
+            vf[(size_t)e] = (float)v;
+        }
+        rp[(size_t)s + 1] = (int32_t)e;
+    }
+    CK(cudaMalloc(&J.rs_rowptr, sizeof(int32_t) * (n + 1)));
+    CK(cudaMalloc(&J.rs_colw, sizeof(uint32_t) * cw.size()));
+    CK(cudaMalloc(&J.rs_valf, sizeof(float) * vf.size()));
+    CK(cudaMemcpy(J.rs_rowptr, rp.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(J.rs_colw, cw.data(), sizeof(uint32_t) * cw.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(J.rs_valf, vf.data(), sizeof(float) * vf.size(), cudaMemcpyHostToDevice));
     return SBX_OK;
 }
 

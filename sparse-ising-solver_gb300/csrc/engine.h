@@ -58,7 +58,12 @@ struct DevCsr {
     double wsum = 0;         // reference csr.sum
     int32_t max_deg = 0;
     std::vector<double> hval;   // host copy of values (xi0)
-    std::vector<int32_t> hrowptr, hcol;
+    std::vector<int32_t> hrowptr, hcol, hperm;
+    // The matrix relabelled into perm order (row and column s = perm slot s),
+    // built on first use by the register + shared resident kernel.
+    int32_t *rs_rowptr = nullptr;
+    uint32_t *rs_colw = nullptr;
+    float *rs_valf = nullptr;
 };
 
 // Control words shared by the kernels of one solve.
@@ -155,6 +160,11 @@ int resident_pick_ka(const SolveDims &d, const DevCsr &J, int requested);
 size_t resident_smem_bytes(const SolveDims &d, int ka);
 cudaError_t launch_resident(const SolveDims &d, const DevCsr &J, Work &w, int ka,
                             int32_t step0, int32_t nsteps, bool first, cudaStream_t s);
+// Register + shared-memory resident kernel (k_resident_rs.cu), 8 agents per
+// CTA, 16-bit fused state: a configuration number > 0 when the shape fits.
+int resident_rs_pick(const SolveDims &d, const DevCsr &J, bool forced);
+cudaError_t launch_resident_rs(const SolveDims &d, const DevCsr &J, Work &w, int cfg, int32_t step0,
+                               int32_t nsteps, bool first, cudaStream_t s);
 
 // TSP kernels (k_tsp.cu).
 struct DevTsp {
