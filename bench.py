@@ -244,6 +244,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--sb-steps", type=int, default=0,
                     help="SB steps per solve (profiling cases use fewer)")
+    ap.add_argument("--profile", type=int, default=0, metavar="STEPS",
+                    help="one solve of STEPS SB steps of the workload and exit, kernels "
+                         "launched directly: the case the ncu summaries capture")
+    ap.add_argument("--kernel", default="auto", choices=["auto", "stream", "resident", "split"],
+                    help="--profile: kernel family")
+    ap.add_argument("--tile", default="", metavar="V,LR,BT,CM",
+                    help="--profile: streaming tile (agents per lane, lanes per row, threads, "
+                         "count mode 1 bytes / 2 bit planes); default: the fixed heuristic")
     ap.add_argument("--legs", default="all", choices=["all", "main"],
                     help="main: only the timed solves of the main precision (profiling)")
     args = ap.parse_args()
@@ -256,6 +264,9 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, wl, rank)
+        return
+    if args.profile:
+        run_profile_case(args, wl)
         return
     if wl["kind"] == "batch":
         run_batch(args, wl, rank, world, local)
@@ -446,6 +457,39 @@ def main():
     if dist is not None:
         dist.destroy_process_group()
 
+
+
+def run_profile_case(args, wl):
+    """--profile STEPS: one solve (batched: one solve_batch) of the workload
+    with STEPS SB steps of its schedule, no CUDA graph, the tile pinned --
+    a small, repeatable case for ncu captures."""
+    import sbx
+    kern = {"auto": sbx.KERNEL_AUTO, "stream": sbx.KERNEL_STREAM, "resident": sbx.KERNEL_RESIDENT,
+            "split": sbx.KERNEL_RESIDENT_SPLIT}[args.kernel]
+    kw = dict(dt=wl["dt"], steps=wl["sb_steps"], run_steps=args.profile, seed=INIT_SEED,
+              precision=sbx.PRECISIONS[wl["precision"]], kernel=kern,
+              flags=sbx.FLAG_NO_GRAPH | sbx.FLAG_NO_TUNE)
+    if args.tile:
+        v, lr, bt, cm = (int(t) for t in args.tile.split(","))
+        kw.update(lane_agents=v, row_lanes=lr, block_threads=bt, count_mode=cm)
+    ctx = sbx.Context(0)
+    if wl["kind"] == "batch":
+        graphs = batch_instances(wl)
+        probs = [ctx.problem(g) for g in graphs]
+        res, _, t = ctx.solve_batch(probs, [wl["agents"]] * len(probs), sbx.params(fused=wl["fused"], **kw))
+        r = res[0]
+    else:
+        inst = build_instance(wl)
+        if wl["kind"] == "maxcut":
+            prob = ctx.problem(inst)
+            kw.update(fused=wl["fused"], update_window=wl["update_window"])
+        else:
+            prob = ctx.tsp_problem(inst["packed"], inst["N"], A=inst["A"], B=inst["B"], C_=inst["C"])
+        r, _ = ctx.solve(prob, sbx.params(agents=wl["agents"], **kw))
+    print(json.dumps({"profile": wl["workload"], "steps_run": r["steps_run"], "kernel": r["kernel_used"],
+                      "tile": [r["lane_agents"], r["row_lanes"], r["block_threads"], r["count_mode"]],
+                      "time_us": r["time_us"]}), flush=True)
+    ctx.close()
 
 
 def run_batch(args, wl, rank, world, local):
