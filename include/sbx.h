@@ -83,6 +83,9 @@ typedef struct sbx_params {
     int32_t count_mode;     /* +-1 weights: 1 byte counters per lane, 2 bit
                                planes per sign word (neighbours split across
                                the word's lanes); 0: autotuned */
+    int32_t staging;        /* state larger than L2, whole-warp rows: 1 direct
+                               loads, 2 rows copied ahead into shared memory
+                               (bulk asynchronous copies); 0: autotuned */
     double target;          /* MaxCut: a cut; > 0 records the per-window best
                                cut (as trace = 1) and times its first reach */
 } sbx_params;
@@ -103,6 +106,7 @@ typedef struct sbx_result {
     int32_t row_lanes;
     int32_t block_threads;
     int32_t count_mode;
+    int32_t staging;
     double kernel_ms;       /* SBX_FLAG_PROFILE: summed hot-kernel time */
     int64_t kernel_launches;/* hot-kernel launches issued by the solve */
     int64_t gpu_launches;   /* all kernel launches issued by the solve */

@@ -28,7 +28,7 @@ using namespace sbx;
 
 // Streaming step tile (agents per lane, lanes per row, threads per CTA).
 struct Tile {
-    int32_t v = 0, lr = 32, bt = 256, cm = 0;
+    int32_t v = 0, lr = 32, bt = 256, cm = 0, st = 0;
 };
 
 struct sbx_problem {
@@ -410,6 +410,18 @@ bool poll_stop(sbx_ctx *ctx, int64_t c, bool force_all)
 
 // ---- streaming step tile
 
+// The state (x and y) is more than half of L2: it streams from DRAM each step.
+bool state_exceeds_half_l2(const SolveDims &d)
+{
+    static int l2 = -1;
+    if (l2 < 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess) l2 = 0;
+    }
+    return 2.0 * (double)d.n * d.Ap * prec_bytes(d.prec) > 0.5 * (double)l2;
+}
+
 // A tile the step kernels are built for (k_step.cuh, step_kw): whole-warp
 // rows take any vector width dividing the padded agents; 16, 8 or 4 lanes
 // per row take the two widest vectors and exactly the padded agents, and
@@ -441,15 +453,20 @@ int pick_tile(sbx_ctx *ctx, SolveDims &d, const DevCsr &J, const sbx_params *pr,
     const bool big = J.unit && J.nchunks > 0;
     const int fv = pr->lane_agents, flr = pr->row_lanes, fbt = pr->block_threads;
     const int fcm = pr->count_mode;   // 1 byte counters, 2 bit planes
+    const int fst = pr->staging;      // 1 direct loads, 2 staged rows
+    // staged rows pay off only when the state streams from DRAM
+    const bool can_stage = J.unit && state_exceeds_half_l2(d);
     std::vector<Tile> cands;
     const int vs[4] = {8, 4, 2, 1}, lrs[4] = {32, 16, 8, 4}, bts[2] = {256, 128};
+    const int st_forced = (fst == 2 && J.unit) ? 1 : 0;   // staging asked for: whole-warp rows only
     for (int cm = 0; cm < (J.unit ? 2 : 1); cm++)
         for (int v : vs)
             for (int lr : lrs)
                 for (int bt : bts) {
                     if ((fv && v != fv) || (flr && lr != flr) || (fbt && bt != fbt) || (fcm && cm != fcm - 1))
                         continue;
-                    if (tile_ok(d, big, v, lr, bt)) cands.push_back(Tile{v, lr, bt, cm});
+                    if (st_forced && lr != 32) continue;
+                    if (tile_ok(d, big, v, lr, bt)) cands.push_back(Tile{v, lr, bt, cm, st_forced});
                 }
     if (cands.empty())
         return fail(ctx, SBX_ERR_ARG, "no streaming tile fits lane_agents / row_lanes / block_threads");
@@ -458,6 +475,7 @@ int pick_tile(sbx_ctx *ctx, SolveDims &d, const DevCsr &J, const sbx_params *pr,
         d.tlr = t.lr;
         d.tbt = t.bt;
         d.tcm = t.cm;
+        d.tst = t.st;
     };
     apply(cands[0]);
     if (cands.size() == 1) return SBX_OK;
@@ -465,13 +483,13 @@ int pick_tile(sbx_ctx *ctx, SolveDims &d, const DevCsr &J, const sbx_params *pr,
         // fixed heuristic: widest dividing vector, whole-warp rows, 256
         // threads, byte counters
         for (const Tile &t : cands)
-            if (t.v == default_v(d) && t.lr == 32 && t.bt == 256 && t.cm == 0) apply(t);
+            if (t.v == default_v(d) && t.lr == 32 && t.bt == 256 && t.cm == 0 && t.st == 0) apply(t);
         return SBX_OK;
     }
     char key[192];
-    snprintf(key, sizeof key, "%lld/%lld/%d/%d/%lld/%d%d%d/%d/%d/%d/%d/%d/%d/%d", (long long)J.n,
+    snprintf(key, sizeof key, "%lld/%lld/%d/%d/%lld/%d%d%d/%d/%d/%d/%d/%d/%d/%d/%d", (long long)J.n,
              (long long)J.nnz, J.max_deg, J.nchunks, (long long)J.nheavy, (int)J.unit, (int)J.skewed,
-             (int)(J.c0r32 != nullptr), d.prec, d.Ap, d.fused, fv, flr, fbt, fcm);
+             (int)(J.c0r32 != nullptr), d.prec, d.Ap, d.fused, fv, flr, fbt, fcm, fst);
     auto &cache = ctx->tiles;
     auto it = cache.find(key);
     if (it != cache.end()) {
@@ -505,8 +523,27 @@ int pick_tile(sbx_ctx *ctx, SolveDims &d, const DevCsr &J, const sbx_params *pr,
     size_t bi = 0;
     for (size_t i = 1; i < cands.size(); i++)
         if (best[i] < best[bi]) bi = i;
-    apply(cands[bi]);
-    cache[key] = cands[bi];
+    Tile win = cands[bi];
+    // staged rows: tried on the winning tile only, when the state streams
+    if (!fst && can_stage && win.lr == 32 && !win.st) {
+        Tile t = win;
+        t.st = 1;
+        float bs = 1e30f;
+        for (int round = 0; round < 2; round++) {
+            apply(t);
+            CK(launch_plain_steps(d, J, w, 1, s));
+            CK(cudaEventRecord(ctx->ev0, s));
+            CK(launch_plain_steps(d, J, w, reps, s));
+            CK(cudaEventRecord(ctx->ev1, s));
+            CK(cudaEventSynchronize(ctx->ev1));
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+            bs = std::min(bs, ms / reps);
+        }
+        if (bs < best[bi]) win = t;
+    }
+    apply(win);
+    cache[key] = win;
     *timed = true;
     return SBX_OK;
 }
@@ -552,10 +589,10 @@ int run_stream(sbx_ctx *ctx, const void *key_obj, const SolveDims &d, const DevC
         int per_chunk = 0;
         if (use_graph) {
             char key[256];
-            snprintf(key, sizeof key, "%p/%lld/%d/%d/%d/%d/%d/%d/%d/%d/%.17g/%llu/%p/%d/%d/%d/%d/%d",
+            snprintf(key, sizeof key, "%p/%lld/%d/%d/%d/%d/%d/%d/%d/%d/%.17g/%llu/%p/%d/%d/%d/%d/%d/%d",
                      key_obj, (long long)d.n, d.A, d.prec, d.period, d.fused, d.uw, d.threshold,
                      (int)d.pdl, d.steps, d.c0, (unsigned long long)g_alloc_gen, (void *)s, d.tv,
-                     d.tlr, d.tbt, d.tcm, d.trace);
+                     d.tlr, d.tbt, d.tcm, d.tst, d.trace);
             if (!ctx->gexec || ctx->gkey != key) {
                 if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
                 ctx->gexec = nullptr;
@@ -695,6 +732,7 @@ int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_r
     CK(cudaStreamSynchronize(s));
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    if (ctl[CTL_ERR]) return fail(ctx, SBX_ERR_CUDA, "a bounded wait in the step kernel gave up");
     memset(res, 0, sizeof *res);
     stats(cut, res);
     res->time_us = ms * 1000.0;
@@ -709,6 +747,7 @@ int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_r
         res->row_lanes = d.tlr;
         res->block_threads = d.tbt;
         res->count_mode = d.tcm + 1;
+        res->staging = d.tst + 1;
     }
     if ((rc = read_trace(ctx, d, ctl[CTL_TRACED], pr->target, res))) return rc;
     if (ka || rs) {
@@ -1105,6 +1144,7 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
             r->row_lanes = d.tlr;
             r->block_threads = d.tbt;
             r->count_mode = d.tcm + 1;
+            r->staging = d.tst + 1;
             if (targets)
                 for (size_t k = 0; k < recs.size(); k++)
                     if (bt[k * c.probs.size() + i] >= targets[gi]) {
@@ -1426,7 +1466,7 @@ int sbx_solve(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
     if (pr->agents < 1 || pr->steps < 0 || !(pr->dt == pr->dt) || pr->precision < 0 ||
         pr->precision > 3 || pr->run_steps < 0 || pr->period < 0 || pr->threshold < 0 ||
         pr->lane_agents < 0 || pr->row_lanes < 0 || pr->block_threads < 0 || pr->count_mode < 0 ||
-        pr->count_mode > 2 || !(pr->target == pr->target))
+        pr->count_mode > 2 || pr->staging < 0 || pr->staging > 2 || !(pr->target == pr->target))
         return fail(ctx, SBX_ERR_ARG, "bad params (agents >= 1, steps >= 0, precision 0..3)");
     if (pr->agents < 2 && !p->tsp) {
         // the reference's std dev divides by agents-1; one agent is allowed

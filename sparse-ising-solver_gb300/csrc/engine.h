@@ -67,7 +67,8 @@ struct DevCsr {
 };
 
 // Control words shared by the kernels of one solve.
-enum Ctl { CTL_STEP = 0, CTL_STOP = 1, CTL_WINDOWS = 2, CTL_NBIF = 3, CTL_TRACED = 4, CTL_N = 8 };
+// CTL_ERR: a kernel gave up a bounded wait (set, never cleared by kernels).
+enum Ctl { CTL_STEP = 0, CTL_STOP = 1, CTL_WINDOWS = 2, CTL_NBIF = 3, CTL_TRACED = 4, CTL_ERR = 5, CTL_N = 8 };
 
 // One window of a traced solve: SB steps run, best cut over the agents of
 // the window spins, nanoseconds since the loop began (device clock).
@@ -123,6 +124,7 @@ struct SolveDims {
     // Ap), lanes per row (32, 16, 8, 4), threads per CTA
     int32_t tv = 0, tlr = 32, tbt = 256;
     int32_t tcm = 0;         // +-1 rows: 0 byte counters per lane, 1 bit planes per word
+    int32_t tst = 0;         // 1: whole-warp rows staged through shared memory (bulk copies)
     int trace = 0;           // per-window best-cut records: 1 one problem, 2 batched
 };
 

@@ -165,6 +165,44 @@ __device__ __forceinline__ Raw<V * sizeof(T)> from_vals(const A (&o)[V])
     return r;
 }
 
+// Bulk asynchronous copies global -> shared with an mbarrier (sm_90+ PTX).
+// Addresses 16-byte aligned, sizes multiples of 16 (the callers' segments are
+// 32 agents x 16 bytes per lane row pieces).
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+// Bounded wait for phase `parity` of the barrier: false when it did not
+// complete within the limit (the caller flags the error).
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    for (uint32_t k = 0; k < (1u << 22); k++) {
+        uint32_t ok;
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(ok)
+                     : "r"(smem_u32(bar)), "r"(parity)
+                     : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
 // x + a*b: one FMA in FP32; in FP64 two separately rounded operations, the
 // reference's arithmetic as the oracle states it.
 __device__ __forceinline__ float madd(float a, float b, float x) { return fmaf(a, b, x); }
@@ -386,15 +424,18 @@ __device__ __forceinline__ void sb_update(double (&x)[V], double (&y)[V], const 
 // Resident CTAs per SM asked of the register allocator (measured on GB300):
 // 6 for heavy-row kernels, 4 for bit-plane counting (its loads in flight
 // need registers), 5 otherwise.
-template <class T, int V, int KIND, bool WIN, int WM, bool BIG, int LR, int CM>
+template <class T, int V, int KIND, bool WIN, int WM, bool BIG, int LR, int CM, int ST>
 __global__ void __launch_bounds__(256, BIG ? 6 : (CM ? 4 : 5)) k_row(const StepP P, const int offset)
 {
     static_assert(LR == 32 || !BIG, "heavy rows are counted by whole warps");
+    static_assert(!ST || (LR == 32 && !WIN && KIND != K_XY), "staged rows: whole-warp rows, plain steps");
     static_assert(LR * V >= 32, "a sign word belongs to one row's lanes");
     using A = typename St<T>::A;
     using R = typename std::conditional<WM == W_F64, double, float>::type;
     using RawT = Raw<V * sizeof(T)>;
-    extern __shared__ uint32_t s_chg[];   // [W] window steps: changed bits of this block
+    // window steps: [W] changed bits of this block; staged steps: the warps'
+    // x, y stages
+    extern __shared__ __align__(16) uint32_t s_chg[];
     pdl_wait();
     if (P.ctl[CTL_STOP]) return;          // block-uniform
     const int step = P.ctl[CTL_STEP] + offset;
@@ -515,27 +556,8 @@ __global__ void __launch_bounds__(256, BIG ? 6 : (CM ? 4 : 5)) k_row(const StepP
     const int64_t ng = (nrows + RW - 1) / RW;
     const int64_t dr = nw / nit;
     const int dit = (int)(nw - dr * nit);
-    int64_t g = w0 / nit;
-    int it = (int)(w0 - g * nit);
-    for (; g < ng; g += dr, it += dit) {
-        if (it >= nit) {
-            it -= nit;
-            g++;
-            if (g >= ng) break;
-        }
-        // lanes of a group past the last row repeat the last row, store nothing
-        const int64_t gi = g * RW + rw;
-        const bool live = RW == 1 || gi < nrows;
-        const int64_t ri = P.row0 + (live ? gi : nrows - 1);
-        const int64_t r = P.order ? (int64_t)__ldg(&P.order[ri]) : ri;
-        const int a0 = it * LR * V + sl * V;
-        const int q = a0 >> 5, off = a0 & 31;
-        const int64_t base = r * P.Ap + a0;
-        uint32_t wp_old = 0;   // window steps: the previous window's word, fetched early
-        if (WIN && (lane & (G - 1)) == 0) wp_old = P.Wp[r * P.W + q];
-        const RawT xr = vload_s<T, V>(xp + base, cs);
-        const RawT yr = vload_s<T, V>(yp + base, cs);
-        A tv[V];
+    // Totals (the force sum_j J_ij s_j) of the item's V agents of row r.
+    auto item_totals = [&](int64_t r, int q, int off, A (&tv)[V]) {
         if (KIND != K_XY) {
             const int32_t e0 = __ldg(&P.rowptr[r]), e1 = __ldg(&P.rowptr[r + 1]);
             const int32_t deg = e1 - e0;
@@ -589,7 +611,99 @@ __global__ void __launch_bounds__(256, BIG ? 6 : (CM ? 4 : 5)) k_row(const StepP
                 for (int v = 0; v < V; v++) tv[v] = (A)tot[v];
             }
         }
+    };
+
+    if constexpr (ST) {
+        // Staged rows (state larger than L2): each warp copies the x, y
+        // segments of its next item into shared memory (bulk asynchronous
+        // copies completing on an mbarrier) while it works on the current
+        // one, so the state's DRAM latency is off the item's critical path.
+        constexpr int SEGB = 32 * V * (int)sizeof(T);
+        static_assert(SEGB % 16 == 0, "bulk copies move 16-byte multiples");
+        __shared__ __align__(8) uint64_t s_bar[8][2];   // 256-thread blocks at most
+        const int wid = threadIdx.x >> 5;
+        unsigned char *stg = (unsigned char *)s_chg + (size_t)wid * 4 * SEGB;
+        if (lane == 0) {
+            mbar_init(&s_bar[wid][0], 1);
+            mbar_init(&s_bar[wid][1], 1);
+            mbar_fence_init();
+        }
+        __syncwarp();
+        auto row_of = [&](int64_t gg) -> int64_t {
+            const int64_t ri = P.row0 + gg;
+            return P.order ? (int64_t)__ldg(&P.order[ri]) : ri;
+        };
+        auto issue = [&](int stage, int64_t rr, int itx) {
+            if (lane == 0) {
+                const int64_t e = rr * P.Ap + (int64_t)itx * 32 * V;
+                mbar_expect_tx(&s_bar[wid][stage], 2 * SEGB);
+                bulk_g2s(stg + stage * 2 * SEGB, xp + e, SEGB, &s_bar[wid][stage]);
+                bulk_g2s(stg + stage * 2 * SEGB + SEGB, yp + e, SEGB, &s_bar[wid][stage]);
+            }
+        };
+        int64_t g = w0 / nit;
+        int it = (int)(w0 - g * nit);
+        int64_t r = 0;
+        if (g < ng) {
+            r = row_of(g);
+            issue(0, r, it);
+        }
+        uint32_t j = 0;
+        while (g < ng) {
+            int64_t gn = g + dr;
+            int itn = it + dit;
+            if (itn >= nit) {
+                itn -= nit;
+                gn++;
+            }
+            const int64_t rn = gn < ng ? row_of(gn) : 0;
+            if (gn < ng) issue((j + 1) & 1, rn, itn);
+            if (!mbar_wait(&s_bar[wid][j & 1], (j >> 1) & 1)) {
+                // never expected: flag it, let the copy in flight land, stop
+                if (lane == 0) atomicExch(&P.ctl[CTL_ERR], 1);
+                if (gn < ng) mbar_wait(&s_bar[wid][(j + 1) & 1], ((j + 1) >> 1) & 1);
+                break;
+            }
+            const int a0 = it * 32 * V + lane * V;
+            const int q = a0 >> 5, off = a0 & 31;
+            const unsigned char *sx = stg + (j & 1) * 2 * SEGB + lane * V * (int)sizeof(T);
+            RawT xr, yr;
+            xr.u = *(const decltype(xr.u) *)sx;
+            yr.u = *(const decltype(yr.u) *)(sx + SEGB);
+            A tv[V];
+            item_totals(r, q, off, tv);
+            finish(r, q, off, r * P.Ap + a0, true, xr, yr, tv, row_c0(r), 0u);
+            __syncwarp();   // this stage is free for the copy two items on
+            g = gn;
+            it = itn;
+            r = rn;
+            j++;
+        }
+    } else {
+    int64_t g = w0 / nit;
+    int it = (int)(w0 - g * nit);
+    for (; g < ng; g += dr, it += dit) {
+        if (it >= nit) {
+            it -= nit;
+            g++;
+            if (g >= ng) break;
+        }
+        // lanes of a group past the last row repeat the last row, store nothing
+        const int64_t gi = g * RW + rw;
+        const bool live = RW == 1 || gi < nrows;
+        const int64_t ri = P.row0 + (live ? gi : nrows - 1);
+        const int64_t r = P.order ? (int64_t)__ldg(&P.order[ri]) : ri;
+        const int a0 = it * LR * V + sl * V;
+        const int q = a0 >> 5, off = a0 & 31;
+        const int64_t base = r * P.Ap + a0;
+        uint32_t wp_old = 0;   // window steps: the previous window's word, fetched early
+        if (WIN && (lane & (G - 1)) == 0) wp_old = P.Wp[r * P.W + q];
+        const RawT xr = vload_s<T, V>(xp + base, cs);
+        const RawT yr = vload_s<T, V>(yp + base, cs);
+        A tv[V];
+        item_totals(r, q, off, tv);
         finish(r, q, off, base, live, xr, yr, tv, row_c0(r), wp_old);
+    }
     }
     if (WIN) {
         __syncthreads();
@@ -658,27 +772,44 @@ cudaError_t step_vl(const SolveDims &d, const DevCsr &J, const StepP &P, int off
         Q.order = J.perm;
     }
     const int64_t items = ((d.n - Q.row0 + RW - 1) / RW + (big ? J.nchunks : 0)) * nit;
-    // count mode of the +-1 rows: byte counters per lane (0) or bit planes (1)
+    // count mode of the +-1 rows: byte counters per lane (0) or bit planes (1);
+    // staged rows (x, y copied ahead into shared memory) for whole-warp rows
+    // of plain steps
     const bool cm = d.tcm != 0;
+    constexpr bool can_st = LR == 32 && !WIN && KIND != K_XY;
+    const bool st = can_st && d.tst != 0 && J.unit;
+    const size_t smem_st = (size_t)(bt / 32) * 4 * 32 * V * sizeof(T);
     if constexpr (LR == 32) {
         if (big) {
-            if (cm) return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, true, 32, 1>, d, items, bt, smem, s, Q, offset);
-            return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, true, 32, 0>, d, items, bt, smem, s, Q, offset);
+            if constexpr (can_st) {
+                if (st) {
+                    if (cm) return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, true, 32, 1, 1>, d, items, bt, smem_st, s, Q, offset);
+                    return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, true, 32, 0, 1>, d, items, bt, smem_st, s, Q, offset);
+                }
+            }
+            if (cm) return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, true, 32, 1, 0>, d, items, bt, smem, s, Q, offset);
+            return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, true, 32, 0, 0>, d, items, bt, smem, s, Q, offset);
         }
     } else {
         if (big) return cudaErrorInvalidValue;
     }
-    if (KIND == K_XY) return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, false, LR, 0>, d, items, bt, smem, s, Q, offset);
+    if (KIND == K_XY) return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, false, LR, 0, 0>, d, items, bt, smem, s, Q, offset);
     if (J.unit) {
         if constexpr (KIND != K_XY) {
-            if (cm) return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, false, LR, 1>, d, items, bt, smem, s, Q, offset);
+            if constexpr (can_st) {
+                if (st) {
+                    if (cm) return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, false, LR, 1, 1>, d, items, bt, smem_st, s, Q, offset);
+                    return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, false, LR, 0, 1>, d, items, bt, smem_st, s, Q, offset);
+                }
+            }
+            if (cm) return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, false, LR, 1, 0>, d, items, bt, smem, s, Q, offset);
         }
-        return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, false, LR, 0>, d, items, bt, smem, s, Q, offset);
+        return launch_grid(k_row<T, V, KIND, WIN, W_UNIT, false, LR, 0, 0>, d, items, bt, smem, s, Q, offset);
     }
     if constexpr (sizeof(T) == 8)
-        return launch_grid(k_row<T, V, KIND, WIN, W_F64, false, LR, 0>, d, items, bt, smem, s, Q, offset);
+        return launch_grid(k_row<T, V, KIND, WIN, W_F64, false, LR, 0, 0>, d, items, bt, smem, s, Q, offset);
     else
-        return launch_grid(k_row<T, V, KIND, WIN, W_F32, false, LR, 0>, d, items, bt, smem, s, Q, offset);
+        return launch_grid(k_row<T, V, KIND, WIN, W_F32, false, LR, 0, 0>, d, items, bt, smem, s, Q, offset);
 }
 
 // Agents per lane by default: a 16-byte vector when the padded agent count

@@ -41,7 +41,7 @@ class Params(C.Structure):
                 ("kernel", C.c_int32), ("agents_per_block", C.c_int32), ("trace", C.c_int32),
                 ("flags", C.c_uint32), ("run_steps", C.c_int32), ("lane_agents", C.c_int32),
                 ("row_lanes", C.c_int32), ("block_threads", C.c_int32), ("count_mode", C.c_int32),
-                ("target", C.c_double)]
+                ("staging", C.c_int32), ("target", C.c_double)]
 
 
 class Result(C.Structure):
@@ -51,7 +51,7 @@ class Result(C.Structure):
                 ("bifurcated", C.c_int64), ("valid", C.c_int64), ("best_agent", C.c_int32),
                 ("kernel_used", C.c_int32), ("agents_per_block", C.c_int32),
                 ("lane_agents", C.c_int32), ("row_lanes", C.c_int32), ("block_threads", C.c_int32),
-                ("count_mode", C.c_int32), ("kernel_ms", C.c_double), ("kernel_launches", C.c_int64),
+                ("count_mode", C.c_int32), ("staging", C.c_int32), ("kernel_ms", C.c_double), ("kernel_launches", C.c_int64),
                 ("gpu_launches", C.c_int64), ("time_to_target_us", C.c_double),
                 ("steps_to_target", C.c_int64)]
 

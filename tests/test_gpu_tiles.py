@@ -247,3 +247,26 @@ def test_dense_unit_rows_count_modes_bitexact_with_oracle(ctx, oracle, agents, c
     ox, oy = oracle_first_steps(oracle, og, A, seed, dt, max_steps, 200, 1)
     np.testing.assert_array_equal(x, ox)
     np.testing.assert_array_equal(y, oy)
+
+
+@pytest.mark.parametrize("prec", [sbx.BF16, sbx.F32, sbx.F64])
+@pytest.mark.parametrize("count_mode", [1, 2])
+def test_staged_rows_give_the_same_state(ctx, prec, count_mode):
+    # rows copied ahead into shared memory (bulk asynchronous copies) against
+    # direct loads: heavy rows (R-MAT) and plain rows, every lane width
+    for g, A in ((sbx.gen_rmat(13, 6, seed=77), 256), (sbx.gen_er(700, 0.02, pm1=True, seed=8), 64)):
+        prob = ctx.problem(g)
+        ref = None
+        for staging in (1, 2):
+            r, cut = ctx.solve(prob, sbx.params(dt=0.5, steps=400, agents=A, seed=5, precision=prec,
+                                                kernel=sbx.KERNEL_STREAM, row_lanes=32,
+                                                count_mode=count_mode, staging=staging))
+            assert r["staging"] == staging
+            x, y, s = ctx.state(g.n, A)
+            if ref is None:
+                ref = (x, y, s, cut)
+                continue
+            np.testing.assert_array_equal(x, ref[0])
+            np.testing.assert_array_equal(y, ref[1])
+            np.testing.assert_array_equal(s, ref[2])
+            np.testing.assert_array_equal(cut, ref[3])
