@@ -126,6 +126,24 @@ struct SolveDims {
     int32_t tcm = 0;         // +-1 rows: 0 byte counters per lane, 1 bit planes per word
     int32_t tst = 0;         // 1: whole-warp rows staged through shared memory (bulk copies)
     int trace = 0;           // per-window best-cut records: 1 one problem, 2 batched
+    int32_t steps_run = 0;   // resident batch: SB steps of the run
+};
+
+// A batch class packed for the resident batch kernel (k_resident_batch.cu):
+// whole instances in bins, rows of a bin by decreasing degree ("slots"), the
+// matrix relabelled into slot order.
+struct DevRb {
+    int32_t *rowptr = nullptr;   // [slots + 1]
+    uint32_t *colw = nullptr;    // columns as slots, bit 31 the weight sign
+    float *valf = nullptr;
+    float *c0 = nullptr;         // dt * xi0 per slot
+    int32_t *perm = nullptr;     // slot -> row
+    int32_t *bin_off = nullptr;  // [nbins + 1]
+    int32_t *cta_bin = nullptr;  // bins, largest first
+    int32_t nbins = 0;
+    int64_t max_bin_rows = 0;
+    bool unit = false;
+    double dt = -1;              // dt of the uploaded c0
 };
 
 // ---- launchers (k_*.cu) ----
@@ -162,6 +180,11 @@ int resident_pick_ka(const SolveDims &d, const DevCsr &J, int requested);
 size_t resident_smem_bytes(const SolveDims &d, int ka);
 cudaError_t launch_resident(const SolveDims &d, const DevCsr &J, Work &w, int ka,
                             int32_t step0, int32_t nsteps, bool first, cudaStream_t s);
+// Resident batch kernel (k_resident_batch.cu): bins hold at most this many
+// rows; one launch runs d.steps_run fused steps of every instance.
+int64_t resident_batch_max_rows();
+cudaError_t launch_resident_batch(const SolveDims &d, const DevRb &B, Work &w, cudaStream_t s);
+
 // Register + shared-memory resident kernel (k_resident_rs.cu), 8 agents per
 // CTA, 16-bit fused state: a configuration number > 0 when the shape fits.
 int resident_rs_pick(const SolveDims &d, const DevCsr &J, bool forced);

@@ -79,3 +79,30 @@ def test_split_resident_refusals(ctx):
     with pytest.raises(sbx.SbxError):
         ctx.solve(ctx.problem(hub), sbx.params(steps=100, agents=64, precision=sbx.BF16,
                                                kernel=sbx.KERNEL_RESIDENT_SPLIT))
+
+
+@pytest.mark.parametrize("prec", [sbx.BF16, sbx.F16])
+def test_resident_batch_equals_streaming_batch(ctx, prec):
+    # instances packed into bins of the resident batch kernel (here more rows
+    # than one bin holds, so several bins) against the streaming batch:
+    # identical per-agent cuts and statistics (batches take integer weights)
+    gs = [sbx.gen_rgg(9000, 8.0, seed=31), sbx.gen_er(8500, 0.002, pm1=True, seed=32),
+          sbx.gen_torus(90, 100, seed=33), sbx.gen_er(300, 0.04, pm1=True, seed=1),
+          sbx.gen_torus(20, 30, seed=3), sbx.gen_er(150, 0.1, pm1=False, seed=5)]
+    agents = [64, 64, 40, 64, 32, 96]
+    probs = [ctx.problem(g) for g in gs]
+    base = dict(dt=0.5, steps=1200, seed=77, precision=prec)
+    res_r, vals_r, _ = ctx.solve_batch(probs, agents, sbx.params(kernel=sbx.KERNEL_RESIDENT, **base))
+    res_s, vals_s, _ = ctx.solve_batch(probs, agents, sbx.params(kernel=sbx.KERNEL_STREAM, **base))
+    assert all(r["kernel_used"] == sbx.KERNEL_RESIDENT for r in res_r)
+    assert all(r["kernel_used"] == sbx.KERNEL_STREAM for r in res_s)
+    np.testing.assert_array_equal(vals_r, vals_s)
+    for a, b in zip(res_r, res_s):
+        for k in ("max", "min", "mean", "std", "ps", "steps_run"):
+            assert a[k] == b[k], k
+    # by itself (AUTO) the resident batch is taken for low-degree classes
+    # (mean degree <= 8), the streaming kernel otherwise
+    res_a, vals_a, _ = ctx.solve_batch(probs, agents, sbx.params(**base))
+    nnz, rows = sum(g.nnz for g in gs), sum(g.n for g in gs)
+    assert res_a[0]["kernel_used"] == (sbx.KERNEL_RESIDENT if nnz <= 8 * rows else sbx.KERNEL_STREAM)
+    np.testing.assert_array_equal(vals_a, vals_r)
