@@ -406,8 +406,9 @@ def main():
         if rp["kernel_used"] == sbx.KERNEL_STREAM:
             bytes_per_launch, kname = b_step, "k_row (one SB step per launch)"
         else:
-            bytes_per_launch = b_step * rp["steps_run"]
-            kname = "resident (whole solve per launch; state on chip, effective bytes)"
+            # on-chip kernels run many steps per launch: B_step per step run
+            bytes_per_launch = b_step * rp["steps_run"] / rp["kernel_launches"]
+            kname = "resident (many steps per launch; state on chip, effective bytes)"
         achieved = bytes_per_launch / per_launch_s / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_kind": peak_kind,

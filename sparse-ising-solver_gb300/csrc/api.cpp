@@ -702,9 +702,26 @@ int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_r
     CK(cudaEventRecord(ctx->ev0, s));
     auto resident = [&](int32_t step0, int32_t nsteps, bool first) {
         return ka ? launch_resident(d, p->J, ctx->w, ka, step0, nsteps, first, s)
-                  : launch_resident_rs(d, p->J, ctx->w, rs, step0, nsteps, first, s);
+                  : launch_resident_rs(d, p->J, ctx->w, rs, step0, nsteps, first, false, s);
     };
-    if (ka || rs) {
+    bool coop_done = false;
+    if (rs && d.uw && nchunks > 0) {
+        // every window in one co-resident launch, the exit decided on the device
+        CK(grow(ctx->w.gbar, ctx->w.cap_gbar, (size_t)1));
+        CK(cudaMemsetAsync(ctx->w.gbar, 0, sizeof(int32_t), s));
+        const cudaError_t e = launch_resident_rs(d, p->J, ctx->w, rs, 0, (int32_t)total, true, true, s);
+        if (e == cudaSuccess) {
+            coop_done = true;
+            launches++;
+            hot++;
+        } else if (e != cudaErrorCooperativeLaunchTooLarge) {
+            CK(e);
+        } else {
+            (void)cudaGetLastError();
+        }
+    }
+    if (coop_done) {
+    } else if (ka || rs) {
         if (d.uw) {
             for (int64_t c = 0; c < std::max<int64_t>(nchunks, 1); c++) {
                 CK(resident((int32_t)(c * d.period), nchunks ? d.period : 0, c == 0));
@@ -1413,7 +1430,7 @@ int sbx_destroy(sbx_ctx *ctx)
     void *ptrs[] = {w.x, w.y, w.x2, w.S[0], w.S[1], w.Wp, w.fin, w.chg, w.newmask, w.stab, w.bif,
                     w.prev, w.ctl, w.wincount, w.visits, w.ab, w.sched, w.eacc, w.cut, w.trace,
                     w.tours, w.valid, w.rjump, w.coef32, w.coef64, w.part, w.rinst, w.trace_t0,
-                    w.btrace, w.hcount};
+                    w.btrace, w.hcount, w.gbar};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);

@@ -93,6 +93,7 @@ struct Work {
     float2 *sched = nullptr;              // TSP (b_t, dt*-(1-a_t)) per step
     uint32_t *part = nullptr;             // heavy-row partial counts
     int32_t *hcount = nullptr;            // heavy rows: finished chunks per (row, segment)
+    int32_t *gbar = nullptr;              // window barrier of co-resident launches
     unsigned long long *eacc = nullptr;   // per-agent cut accumulators
     double *cut = nullptr;                // per-agent cuts
     TraceRec *trace = nullptr;            // per-window records; trace_t0: loop start
@@ -106,7 +107,7 @@ struct Work {
     size_t cap_x = 0, cap_y = 0, cap_x2 = 0, cap_S0 = 0, cap_S1 = 0, cap_Wp = 0, cap_fin = 0,
            cap_chg = 0, cap_new = 0, cap_stab = 0, cap_bif = 0, cap_prev = 0, cap_ctl = 0,
            cap_win = 0, cap_visits = 0, cap_ab = 0, cap_sched = 0, cap_eacc = 0, cap_cut = 0,
-           cap_trace = 0, cap_t0 = 0, cap_btrace = 0, cap_tours = 0, cap_valid = 0, cap_rj = 0, cap_c32 = 0, cap_c64 = 0, cap_part = 0, cap_rinst = 0, cap_hcount = 0;
+           cap_trace = 0, cap_t0 = 0, cap_btrace = 0, cap_tours = 0, cap_valid = 0, cap_rj = 0, cap_c32 = 0, cap_c64 = 0, cap_part = 0, cap_rinst = 0, cap_hcount = 0, cap_gbar = 0;
     bool rjump_ready = false;
 };
 
@@ -188,8 +189,11 @@ cudaError_t launch_resident_batch(const SolveDims &d, const DevRb &B, Work &w, c
 // Register + shared-memory resident kernel (k_resident_rs.cu), 8 agents per
 // CTA, 16-bit fused state: a configuration number > 0 when the shape fits.
 int resident_rs_pick(const SolveDims &d, const DevCsr &J, bool forced);
+// coop: the update-window mode's windows in one co-resident launch (a
+// bounded barrier per window); cudaErrorCooperativeLaunchTooLarge when the
+// CTAs cannot all be resident.
 cudaError_t launch_resident_rs(const SolveDims &d, const DevCsr &J, Work &w, int cfg, int32_t step0,
-                               int32_t nsteps, bool first, cudaStream_t s);
+                               int32_t nsteps, bool first, bool coop, cudaStream_t s);
 
 // TSP kernels (k_tsp.cu).
 struct DevTsp {

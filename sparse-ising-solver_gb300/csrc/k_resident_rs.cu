@@ -32,6 +32,8 @@ struct RsP {
     uint8_t *bif, *prev;
     int32_t *ctl;
     int32_t *wincount;                  // bifurcated agents after each window
+    int32_t *gbar;                      // co-resident launch: CTAs past each window
+    int32_t coop;                       // 1: all windows in one co-resident launch
     int32_t n, A, Ap, W, period, threshold, uw;
     int32_t step0, nsteps, first, unit;
     float c0;
@@ -182,6 +184,7 @@ __global__ void __launch_bounds__(NT, 1) k_resident_rs(const RsP P)
     }
     __syncthreads();
 
+    int32_t nrun = P.nsteps;   // steps run (fewer at an update-window exit)
     for (int32_t it = 0; it < P.nsteps; it++) {
         const int32_t k = k0 + it;
         const uint8_t *Sin = (k & 1) ? Sb1 : Sb0;
@@ -245,6 +248,35 @@ __global__ void __launch_bounds__(NT, 1) k_resident_rs(const RsP P)
                 }
             }
             if (tid == 0) s_chg = 0;
+            if (P.uw && P.coop) {
+                // The update-window exit inside one co-resident launch: after
+                // every CTA has counted its bifurcated agents for this window,
+                // all of them read the total (src/ising.cu:200-211).  The
+                // barrier's wait is bounded; giving up flags an error.
+                const int widx = (k + 1) / P.period - 1;
+                __syncthreads();
+                if (tid == 0) {
+                    __threadfence();
+                    atomicAdd(P.gbar, 1);
+                    const int target = (int)gridDim.x * (widx + 1);
+                    uint32_t spins = 0;
+                    while (atomicAdd(P.gbar, 0) < target) {
+                        if (++spins > (1u << 26)) {
+                            atomicExch(&P.ctl[CTL_ERR], 1);
+                            s_stop = 1;
+                            break;
+                        }
+                        __nanosleep(64);
+                    }
+                    __threadfence();
+                    if (!s_stop && atomicAdd(&P.wincount[widx], 0) == P.A) s_stop = 2;
+                }
+                __syncthreads();
+                if (s_stop) {
+                    nrun = it + 1;
+                    break;
+                }
+            }
         }
         __syncthreads();
     }
@@ -272,8 +304,9 @@ __global__ void __launch_bounds__(NT, 1) k_resident_rs(const RsP P)
         P.prev[a] = s_prev[tid];
     }
     if (blockIdx.x == 0 && tid == 0) {
-        P.ctl[CTL_STEP] = P.step0 + P.nsteps;
-        P.ctl[CTL_WINDOWS] = (P.step0 + P.nsteps) / P.period;
+        P.ctl[CTL_STEP] = P.step0 + nrun;
+        P.ctl[CTL_WINDOWS] = (P.step0 + nrun) / P.period;
+        if (s_stop == 2) P.ctl[CTL_STOP] = 1;
     }
 }
 
@@ -293,6 +326,18 @@ size_t rs_smem(int64_t n, const RsCfg &c)
 template <class T, int NT, int RR>
 cudaError_t launch_rs_t(const RsP &P, size_t smem, int grid, cudaStream_t s, bool pdl)
 {
+    if (P.coop) {
+        // every CTA must be resident at once for the window barrier
+        int per_sm = 0, nsm = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaError_t e = cudaFuncSetAttribute(k_resident_rs<T, NT, RR>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resident_rs<T, NT, RR>, NT, smem);
+        if (e != cudaSuccess) return e;
+        if ((int64_t)per_sm * nsm < grid) return cudaErrorCooperativeLaunchTooLarge;
+    }
     cudaError_t e = cudaFuncSetAttribute(k_resident_rs<T, NT, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
@@ -302,10 +347,15 @@ cudaError_t launch_rs_t(const RsP &P, size_t smem, int grid, cudaStream_t s, boo
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
+    if (P.coop) {
+        at[0].id = cudaLaunchAttributeCooperative;
+        at[0].val.cooperative = 1;
+    } else {
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+    }
     cfg.attrs = at;
-    cfg.numAttrs = pdl ? 1 : 0;
+    cfg.numAttrs = (pdl || P.coop) ? 1 : 0;
     return cudaLaunchKernelEx(&cfg, k_resident_rs<T, NT, RR>, P);
 }
 
@@ -339,7 +389,7 @@ int resident_rs_pick(const SolveDims &d, const DevCsr &J, bool forced)
 }
 
 cudaError_t launch_resident_rs(const SolveDims &d, const DevCsr &J, Work &w, int cfg, int32_t step0,
-                               int32_t nsteps, bool first, cudaStream_t s)
+                               int32_t nsteps, bool first, bool coop, cudaStream_t s)
 {
     if (cfg < 1) return cudaErrorInvalidValue;
     RsP P;
@@ -358,6 +408,8 @@ cudaError_t launch_resident_rs(const SolveDims &d, const DevCsr &J, Work &w, int
     P.prev = w.prev;
     P.ctl = w.ctl;
     P.wincount = w.wincount;
+    P.gbar = w.gbar;
+    P.coop = (coop && d.uw && w.gbar) ? 1 : 0;
     P.n = (int32_t)d.n;
     P.A = d.A;
     P.Ap = d.Ap;
