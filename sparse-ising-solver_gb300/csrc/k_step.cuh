@@ -208,6 +208,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
 __device__ __forceinline__ float madd(float a, float b, float x) { return fmaf(a, b, x); }
 __device__ __forceinline__ double madd(double a, double b, double x) { return __dadd_rn(x, __dmul_rn(a, b)); }
 
+// Word of a sign-plane row: row col, word offset already in Sq.  The byte
+// offset is a 32 x 32 -> 64-bit product (col * 4W), one widening multiply-add
+// with the base.
+__device__ __forceinline__ uint32_t plane_ld(const uint32_t *Sq, uint32_t col, int32_t W)
+{
+    const uint32_t wb = (uint32_t)W * 4u;
+    return __ldg((const uint32_t *)((const char *)Sq + (uint64_t)col * (uint64_t)wb));
+}
+
 // Twice the sign bits of a nibble, one per byte: byte i of the result is
 // 2 * bit i.  Byte counters of +-1 neighbours then hold 2 * count (<= 254 for
 // up to kHeavy = 127 neighbours).
@@ -232,7 +241,7 @@ __device__ __forceinline__ void count_unit(const StepP &P, const uint32_t *Sq, i
         for (int k = 0; k < m; k++) {
             const uint32_t cw = __shfl_sync(FULL, mycw, k, LR);
             if (LR == 32 || cb + k < dw) {
-                const uint32_t word = __ldg(Sq + (size_t)(cw & 0x7fffffffu) * (size_t)P.W);
+                const uint32_t word = plane_ld(Sq, cw & 0x7fffffffu, P.W);
                 // weight sign -> all-ones mask; unused high bits only reach
                 // counter bytes that are never read
                 const uint32_t bits = (word >> off) ^ (uint32_t)((int32_t)cw >> 31);
@@ -289,7 +298,7 @@ __device__ __forceinline__ void count_bits(const StepP &P, const uint32_t *Sq, i
                 w[t * KPL + kk] = 0u;
                 if (cb + t * LR < dmax) {
                     // past the row's end cw is 0: row 0 is read, the term dropped
-                    const uint32_t word = __ldg(Sq + (size_t)(cw & 0x7fffffffu) * (size_t)P.W);
+                    const uint32_t word = plane_ld(Sq, cw & 0x7fffffffu, P.W);
                     w[t * KPL + kk] = (cb + t * LR + src < dw) ? (word ^ (uint32_t)((int32_t)cw >> 31)) : 0u;
                 }
             }
@@ -596,7 +605,7 @@ __global__ void __launch_bounds__(256, BIG ? 6 : (CM ? 4 : 5)) k_row(const StepP
                         const uint32_t cw = __shfl_sync(FULL, mycw, k, LR);
                         const R wv = __shfl_sync(FULL, myv, k, LR);
                         if (LR == 32 || cb + k < deg) {
-                            const uint32_t word = __ldg(Sq + (size_t)(cw & 0x7fffffffu) * (size_t)P.W);
+                            const uint32_t word = plane_ld(Sq, cw & 0x7fffffffu, P.W);
                             const uint32_t bits = (word >> off) & VM;
 #pragma unroll
                             for (int v = 0; v < V; v++) {
