@@ -203,6 +203,7 @@ int upload_csr(sbx_ctx *ctx, DevCsr &J, int64_t n, int64_t nnz, const int32_t *r
     J.n = n;
     J.nnz = nnz;
     J.unit = unit;
+    J.allpos = unit && std::all_of(val, val + nnz, [](double v) { return v > 0; });
     J.integer = integer;
     J.wsum = wsum;
     J.max_deg = maxdeg;

@@ -54,6 +54,7 @@ struct DevCsr {
     int32_t *iagents = nullptr;
     double *iwsum = nullptr;
     bool unit = false;       // all |w| == 1
+    bool allpos = false;     // all w == +1 (unit, no sign bits)
     bool integer = false;    // all integer-valued, small enough for int32 sums
     double wsum = 0;         // reference csr.sum
     int32_t max_deg = 0;

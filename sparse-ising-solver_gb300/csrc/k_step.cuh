@@ -49,6 +49,7 @@ struct StepP {
     int64_t n;
     int32_t W, Ap, nchunks;
     int32_t stream_state;                 // state larger than L2: x, y loads/stores evict first
+    int32_t allpos;                       // every weight is +1: no sign bits in colw
     double c0;
 };
 
@@ -227,9 +228,9 @@ __device__ __forceinline__ uint32_t spread2x(uint32_t nib) { return (nib * 0x004
 // each neighbour's row of the plane and adds 2 * (bit ^ weight sign) into
 // byte counters lo (agents 0..3) / hi (4..7).  Counts agents whose neighbour
 // term is -1: the force is 2 * count - degree (src/kernels.cu:247-255).
-template <int V, int LR>
-__device__ __forceinline__ void count_unit(const StepP &P, const uint32_t *Sq, int off, int32_t e0,
-                                           int32_t dw, int sl, uint32_t &lo, uint32_t &hi)
+template <int V, int LR, bool NEG>
+__device__ __forceinline__ void count_unit_s(const StepP &P, const uint32_t *Sq, int off, int32_t e0,
+                                             int32_t dw, int sl, uint32_t &lo, uint32_t &hi)
 {
     int32_t dmax = dw;
     if constexpr (LR < 32) dmax = __reduce_max_sync(FULL, dw);
@@ -241,15 +242,24 @@ __device__ __forceinline__ void count_unit(const StepP &P, const uint32_t *Sq, i
         for (int k = 0; k < m; k++) {
             const uint32_t cw = __shfl_sync(FULL, mycw, k, LR);
             if (LR == 32 || cb + k < dw) {
-                const uint32_t word = plane_ld(Sq, cw & 0x7fffffffu, P.W);
+                // all weights +1: bit 31 is clear, no sign to apply
+                const uint32_t word = plane_ld(Sq, NEG ? (cw & 0x7fffffffu) : cw, P.W);
                 // weight sign -> all-ones mask; unused high bits only reach
                 // counter bytes that are never read
-                const uint32_t bits = (word >> off) ^ (uint32_t)((int32_t)cw >> 31);
+                uint32_t bits = word >> off;
+                if (NEG) bits ^= (uint32_t)((int32_t)cw >> 31);
                 lo += spread2x(bits & 0xfu);
                 if (V == 8) hi += spread2x((bits >> 4) & 0xfu);
             }
         }
     }
+}
+template <int V, int LR>
+__device__ __forceinline__ void count_unit(const StepP &P, const uint32_t *Sq, int off, int32_t e0,
+                                           int32_t dw, int sl, uint32_t &lo, uint32_t &hi)
+{
+    if (P.allpos) count_unit_s<V, LR, false>(P, Sq, off, e0, dw, sl, lo, hi);
+    else count_unit_s<V, LR, true>(P, Sq, off, e0, dw, sl, lo, hi);
 }
 
 // Bit-sliced counting of the same quantity for rows with many neighbours:
@@ -260,9 +270,9 @@ __device__ __forceinline__ void count_unit(const StepP &P, const uint32_t *Sq, i
 // then summed across the group (butterfly of shuffles and bit-sliced adds)
 // and each lane takes out its V agents as byte counters holding 2 * count,
 // the form count_unit leaves.  Counts stay below 128 (kHeavy = 127).
-template <int V, int LR>
-__device__ __forceinline__ void count_bits(const StepP &P, const uint32_t *Sq, int off, int32_t e0,
-                                           int32_t dw, int sl, uint32_t &lo, uint32_t &hi)
+template <int V, int LR, bool NEG>
+__device__ __forceinline__ void count_bits_s(const StepP &P, const uint32_t *Sq, int off, int32_t e0,
+                                             int32_t dw, int sl, uint32_t &lo, uint32_t &hi)
 {
     constexpr int G = 32 / V;
     static_assert(LR % G == 0, "a row's lanes hold whole words");
@@ -298,8 +308,8 @@ __device__ __forceinline__ void count_bits(const StepP &P, const uint32_t *Sq, i
                 w[t * KPL + kk] = 0u;
                 if (cb + t * LR < dmax) {
                     // past the row's end cw is 0: row 0 is read, the term dropped
-                    const uint32_t word = plane_ld(Sq, cw & 0x7fffffffu, P.W);
-                    w[t * KPL + kk] = (cb + t * LR + src < dw) ? (word ^ (uint32_t)((int32_t)cw >> 31)) : 0u;
+                    const uint32_t word = plane_ld(Sq, NEG ? (cw & 0x7fffffffu) : cw, P.W);
+                    w[t * KPL + kk] = (cb + t * LR + src < dw) ? (NEG ? word ^ (uint32_t)((int32_t)cw >> 31) : word) : 0u;
                 }
             }
         }
@@ -345,6 +355,13 @@ __device__ __forceinline__ void count_bits(const StepP &P, const uint32_t *Sq, i
         lo += ((b & 0xfu) * (0x00204081u << (i + 1))) & (0x01010101u << (i + 1));
         if (V == 8) hi += (((b >> 4) & 0xfu) * (0x00204081u << (i + 1))) & (0x01010101u << (i + 1));
     }
+}
+template <int V, int LR>
+__device__ __forceinline__ void count_bits(const StepP &P, const uint32_t *Sq, int off, int32_t e0,
+                                           int32_t dw, int sl, uint32_t &lo, uint32_t &hi)
+{
+    if (P.allpos) count_bits_s<V, LR, false>(P, Sq, off, e0, dw, sl, lo, hi);
+    else count_bits_s<V, LR, true>(P, Sq, off, e0, dw, sl, lo, hi);
 }
 
 // The SB update of V agents from their totals (the force sum_j J_ij s_j):

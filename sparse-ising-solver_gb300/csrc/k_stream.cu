@@ -164,6 +164,7 @@ StepP make_step(const SolveDims &d, const DevCsr &J, Work &w)
     P.chunk_row = J.chunk_row;
     P.part = (uint2 *)w.part;
     P.hcount = w.hcount;
+    P.allpos = J.allpos ? 1 : 0;
     P.nchunks = J.nchunks;
     P.order = nullptr;   // set per kernel (step_vl)
     P.row0 = 0;
