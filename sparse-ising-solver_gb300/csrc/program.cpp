@@ -10,7 +10,8 @@
 // Options after the positional arguments (all optional):
 //   --seed=N         srand seed (default: time(0), as the reference)
 //   --precision=P    f32 (default) | bf16 | f16 | f64
-//   --kernel=K       auto (default) | stream | resident
+//   --kernel=K       auto (default) | stream | resident | split (registers +
+//                    shared memory, 16-bit fused state)
 //   --period=N       steps per window (default: the reference's)
 //   --device=N       CUDA device (default 0)
 //   --compat-stoi    parse time_step with std::stoi as the reference does
@@ -162,7 +163,11 @@ int main(int argc, char *argv[])
         const std::string v = eq == std::string::npos ? "" : a.substr(eq + 1);
         if (k == "seed") o.seed = (unsigned)std::stoul(v);
         else if (k == "precision") o.precision = v == "bf16" ? SBX_BF16 : v == "f16" ? SBX_F16 : v == "f64" ? SBX_F64 : SBX_F32;
-        else if (k == "kernel") o.kernel = v == "stream" ? SBX_KERNEL_STREAM : v == "resident" ? SBX_KERNEL_RESIDENT : SBX_KERNEL_AUTO;
+        else if (k == "kernel")
+            o.kernel = v == "stream"     ? SBX_KERNEL_STREAM
+                       : v == "resident" ? SBX_KERNEL_RESIDENT
+                       : v == "split"    ? SBX_KERNEL_RESIDENT_SPLIT
+                                         : SBX_KERNEL_AUTO;
         else if (k == "period") o.period = std::stoi(v);
         else if (k == "device") o.device = std::stoi(v);
         else if (k == "compat-stoi") o.compat_stoi = true;
