@@ -56,6 +56,16 @@ GRAPH_SEED, INIT_SEED = 1234, 1
 PBYTES = {"f32": 4, "bf16": 2, "f16": 2, "f64": 8}
 
 
+# DRAM traffic (read + write bytes) per launch of each workload's dominant
+# kernel, from the ncu captures summarised in profiles/ (the same kernel and
+# tile the bench runs; the resident kernels' launch covers the whole solve).
+TRAFFIC = {
+    "torus": (45.85e6, "profiles/k_resident_rs_bf16_torus100x100.md (20,000-step launch)"),
+    "rmat20": (2.2139e9, "profiles/k_row_bf16_rmat20.md"),
+    "batch512": (1.3393e9, "profiles/k_row_bf16_batch512.md"),
+}
+
+
 def load_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -410,8 +420,10 @@ def main():
             bytes_per_launch = b_step * rp["steps_run"] / rp["kernel_launches"]
             kname = "resident (many steps per launch; state on chip, effective bytes)"
         achieved = bytes_per_launch / per_launch_s / 1e9
+        tr = TRAFFIC.get(args.workload)
         roof = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_kind": peak_kind,
+                "frac": achieved / peaks["hbm_gbs"], "traffic": tr[0] if tr else None,
+                "traffic_source": tr[1] if tr else None, "peak_kind": peak_kind,
                 "kernel": kname, "bytes_per_launch": bytes_per_launch,
                 "launch_us": per_launch_s * 1e6, "launches": rp["kernel_launches"]}
 
@@ -586,9 +598,10 @@ def run_batch(args, wl, rank, world, local):
     if rp[0]["kernel_ms"] > 0:
         per_launch_s = rp[0]["kernel_ms"] / 1000.0 / rp[0]["steps_run"]
         achieved = b_step / per_launch_s / 1e9
+        tr = TRAFFIC["batch512"]
         roof = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_kind": peak_kind,
-                "kernel": "k_row (+k_heavy) per SB step over all instances",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": tr[0], "traffic_source": tr[1],
+                "peak_kind": peak_kind, "kernel": "k_row per SB step over all instances",
                 "bytes_per_launch": b_step, "launch_us": per_launch_s * 1e6}
     if rank == 0:
         line = {
