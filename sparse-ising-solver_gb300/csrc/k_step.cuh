@@ -75,7 +75,6 @@ template <> struct Coef<double> {
     }
 };
 
-__device__ __forceinline__ uint32_t spread4(uint32_t nib) { return (nib * 0x00204081u) & 0x01010101u; }
 
 // V consecutive storage elements moved as one naturally aligned vector.
 template <int B> struct Raw;
@@ -348,12 +347,32 @@ __device__ __forceinline__ void count_bits_s(const StepP &P, const uint32_t *Sq,
             }
         }
     }
-    // this lane's V agents: bit k of plane i -> 2^(i+1) in byte k
+    if constexpr (V == 8) {
+        // this lane's byte of every plane, gathered into 64 bits (byte i =
+        // plane i), then an 8x8 bit transpose: byte k = agent k's count
+        static_assert(NP <= 8, "planes fit the 8x8 block");
+        const uint32_t sel = (uint32_t)off >> 3;
+        const uint32_t s01 = sel | ((sel + 4) << 4);
+        const uint32_t g0 = __byte_perm(__byte_perm(p[0], p[1], s01), __byte_perm(p[2], p[3], s01), 0x5410);
+        const uint32_t g1 = __byte_perm(__byte_perm(p[4], p[5], s01), __byte_perm(p[6], 0u, sel | 0x4440u), 0x5410);
+        uint64_t x = ((uint64_t)g1 << 32) | g0;
+        uint64_t t;
+        t = (x ^ (x >> 7)) & 0x00AA00AA00AA00AAull;
+        x ^= t ^ (t << 7);
+        t = (x ^ (x >> 14)) & 0x0000CCCC0000CCCCull;
+        x ^= t ^ (t << 14);
+        t = (x ^ (x >> 28)) & 0x00000000F0F0F0F0ull;
+        x ^= t ^ (t << 28);
+        // counts < 128: doubling stays inside each byte
+        lo += (uint32_t)x << 1;
+        hi += (uint32_t)(x >> 32) << 1;
+    } else {
+        // this lane's V agents: bit k of plane i -> 2^(i+1) in byte k
 #pragma unroll
-    for (int i = 0; i < NP; i++) {
-        const uint32_t b = p[i] >> off;
-        lo += ((b & 0xfu) * (0x00204081u << (i + 1))) & (0x01010101u << (i + 1));
-        if (V == 8) hi += (((b >> 4) & 0xfu) * (0x00204081u << (i + 1))) & (0x01010101u << (i + 1));
+        for (int i = 0; i < NP; i++) {
+            const uint32_t b = p[i] >> off;
+            lo += ((b & 0xfu) * (0x00204081u << (i + 1))) & (0x01010101u << (i + 1));
+        }
     }
 }
 template <int V, int LR>
