@@ -82,7 +82,10 @@ typedef struct sbx_params {
     int32_t block_threads;  /* threads per CTA: 128 or 256 */
     int32_t count_mode;     /* +-1 weights: 1 byte counters per lane, 2 bit
                                planes per sign word (neighbours split across
-                               the word's lanes); 0: autotuned */
+                               the word's lanes), 3 mixed (rows with more than
+                               127 neighbours present: bit planes for rows of
+                               12 or more neighbours, byte counters below);
+                               0: autotuned */
     int32_t staging;        /* state larger than L2, whole-warp rows: 1 direct
                                loads, 2 rows copied ahead into shared memory
                                (bulk asynchronous copies); 0: autotuned */

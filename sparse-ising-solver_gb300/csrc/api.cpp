@@ -154,6 +154,7 @@ void free_csr(DevCsr &J)
     J.hchunk = J.chunk_row = nullptr;
     J.nchunks = 0;
     J.nheavy = 0;
+    J.niso = 0;
     J.rowptr = nullptr;
     J.colw = nullptr;
     J.vald = nullptr;
@@ -208,6 +209,8 @@ int upload_csr(sbx_ctx *ctx, DevCsr &J, int64_t n, int64_t nnz, const int32_t *r
     J.wsum = wsum;
     J.max_deg = maxdeg;
     J.skewed = (double)maxdeg > 8.0 * std::max(1.0, (double)nnz / (double)n);
+    J.niso = 0;
+    for (int64_t r = 0; r < n; r++) J.niso += rowptr[r + 1] == rowptr[r];
     J.hval.assign(val, val + nnz);
     J.hrowptr.assign(rowptr, rowptr + n + 1);
     J.hcol.assign(col, col + nnz);
@@ -455,14 +458,15 @@ int pick_tile(sbx_ctx *ctx, SolveDims &d, const DevCsr &J, const sbx_params *pr,
     *timed = false;
     const bool big = J.unit && J.nchunks > 0;
     const int fv = pr->lane_agents, flr = pr->row_lanes, fbt = pr->block_threads;
-    const int fcm = pr->count_mode;   // 1 byte counters, 2 bit planes
+    const int fcm = pr->count_mode;   // 1 byte counters, 2 bit planes, 3 mixed
     const int fst = pr->staging;      // 1 direct loads, 2 staged rows
     // staged rows pay off only when the state streams from DRAM
     const bool can_stage = J.unit && state_exceeds_half_l2(d);
     std::vector<Tile> cands;
     const int vs[4] = {8, 4, 2, 1}, lrs[4] = {32, 16, 8, 4}, bts[2] = {256, 128};
     const int st_forced = (fst == 2 && J.unit) ? 1 : 0;   // staging asked for: whole-warp rows only
-    for (int cm = 0; cm < (J.unit ? 2 : 1); cm++)
+    // mixed counting exists in the heavy-row kernels only
+    for (int cm = 0; cm < (J.unit ? (big ? 3 : 2) : 1); cm++)
         for (int v : vs)
             for (int lr : lrs)
                 for (int bt : bts) {
@@ -472,7 +476,7 @@ int pick_tile(sbx_ctx *ctx, SolveDims &d, const DevCsr &J, const sbx_params *pr,
                     if (tile_ok(d, big, v, lr, bt)) cands.push_back(Tile{v, lr, bt, cm, st_forced});
                 }
     if (cands.empty())
-        return fail(ctx, SBX_ERR_ARG, "no streaming tile fits lane_agents / row_lanes / block_threads");
+        return fail(ctx, SBX_ERR_ARG, "no streaming tile fits lane_agents / row_lanes / block_threads / count_mode");
     auto apply = [&](const Tile &t) {
         d.tv = t.v;
         d.tlr = t.lr;
@@ -620,7 +624,7 @@ int run_stream(sbx_ctx *ctx, const void *key_obj, const SolveDims &d, const DevC
         } else {
             cudaEvent_t *evs = nullptr;
             if (profile) {
-                while ((int)ctx->prof.size() < 2 * d.period) {
+                while ((int)ctx->prof.size() < 2 * d.period + 2) {
                     cudaEvent_t e;
                     CK(cudaEventCreate(&e));
                     ctx->prof.push_back(e);
@@ -631,7 +635,9 @@ int run_stream(sbx_ctx *ctx, const void *key_obj, const SolveDims &d, const DevC
                 CK(launch_chunk(d, J, ctx->w, s, &launches, evs));
                 if (profile) {
                     CK(cudaStreamSynchronize(s));
-                    for (int i = 0; i < d.period; i++) {
+                    // the step kernels, and the isolated rows' window kernel
+                    for (int i = 0; i <= d.period; i++) {
+                        if (i == d.period && !(d.fused && J.niso)) break;
                         float t = 0;
                         CK(cudaEventElapsedTime(&t, evs[2 * i], evs[2 * i + 1]));
                         kernel_ms += t;
@@ -1622,7 +1628,7 @@ int sbx_solve(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
     if (pr->agents < 1 || pr->steps < 0 || !(pr->dt == pr->dt) || pr->precision < 0 ||
         pr->precision > 3 || pr->run_steps < 0 || pr->period < 0 || pr->threshold < 0 ||
         pr->lane_agents < 0 || pr->row_lanes < 0 || pr->block_threads < 0 || pr->count_mode < 0 ||
-        pr->count_mode > 2 || pr->staging < 0 || pr->staging > 2 || !(pr->target == pr->target))
+        pr->count_mode > 3 || pr->staging < 0 || pr->staging > 2 || !(pr->target == pr->target))
         return fail(ctx, SBX_ERR_ARG, "bad params (agents >= 1, steps >= 0, precision 0..3)");
     if (pr->agents < 2 && !p->tsp) {
         // the reference's std dev divides by agents-1; one agent is allowed

@@ -25,6 +25,13 @@ struct RandInst {
 // never overflow.
 constexpr int kHeavy = 127;
 
+// Mixed count mode (kernels with heavy rows): light rows of at least this
+// many neighbours are counted in bit planes, shorter ones in byte counters.
+#ifndef SBX_BITS_MIN
+#define SBX_BITS_MIN 12
+#endif
+constexpr int kBitsMin = SBX_BITS_MIN;
+
 inline size_t prec_bytes(int p) { return p == P_F64 ? 8 : p == P_F32 ? 4 : 2; }
 
 // MaxCut / QUBO matrix on the device.  colw holds the column index; when every
@@ -39,6 +46,7 @@ struct DevCsr {
     int32_t *perm = nullptr; // rows in decreasing degree (resident kernel order)
     bool skewed = false;     // max degree > 8x mean: the step kernel visits rows in perm order
     int64_t nheavy = 0;      // heavy rows: the first nheavy entries of perm
+    int64_t niso = 0;        // isolated rows (degree 0): the last niso entries of perm
     // Heavy rows (unit weights, degree > kHeavy) are split into chunks of
     // kHeavy neighbours, each counted by its own work item of the step kernel.
     int32_t *hchunk = nullptr;    // per row: first chunk of a heavy row, else -1
@@ -125,7 +133,7 @@ struct SolveDims {
     // streaming step tile: agents per lane (0: widest vector that divides
     // Ap), lanes per row (32, 16, 8, 4), threads per CTA
     int32_t tv = 0, tlr = 32, tbt = 256;
-    int32_t tcm = 0;         // +-1 rows: 0 byte counters per lane, 1 bit planes per word
+    int32_t tcm = 0;         // +-1 rows: 0 byte counters per lane, 1 bit planes per word, 2 mixed
     int32_t tst = 0;         // 1: whole-warp rows staged through shared memory (bulk copies)
     int trace = 0;           // per-window best-cut records: 1 one problem, 2 batched
     int32_t steps_run = 0;   // resident batch: SB steps of the run

@@ -50,6 +50,10 @@ struct StepP {
     int32_t W, Ap, nchunks;
     int32_t stream_state;                 // state larger than L2: x, y loads/stores evict first
     int32_t allpos;                       // every weight is +1: no sign bits in colw
+    int32_t bits_min;                     // heavy-row kernels: light rows of this degree or more
+                                          // are counted in bit planes (INT32_MAX: none)
+    int64_t niso;                         // isolated rows left to k_iso: the last niso entries of
+                                          // order, which the row items then skip
     double c0;
 };
 
@@ -59,6 +63,11 @@ cudaError_t step_f32(const SolveDims &d, const DevCsr &J, const StepP &P, int ki
 cudaError_t step_bf16(const SolveDims &d, const DevCsr &J, const StepP &P, int kind, bool win, int offset, cudaStream_t s);
 cudaError_t step_f16(const SolveDims &d, const DevCsr &J, const StepP &P, int kind, bool win, int offset, cudaStream_t s);
 cudaError_t step_f64(const SolveDims &d, const DevCsr &J, const StepP &P, int kind, bool win, int offset, cudaStream_t s);
+// One window of fused steps (d.period) of the isolated rows (k_iso).
+cudaError_t iso_f32(const SolveDims &d, const DevCsr &J, const StepP &P, cudaStream_t s);
+cudaError_t iso_bf16(const SolveDims &d, const DevCsr &J, const StepP &P, cudaStream_t s);
+cudaError_t iso_f16(const SolveDims &d, const DevCsr &J, const StepP &P, cudaStream_t s);
+cudaError_t iso_f64(const SolveDims &d, const DevCsr &J, const StepP &P, cudaStream_t s);
 
 namespace {
 
@@ -597,7 +606,7 @@ __global__ void __launch_bounds__(256, BIG ? 6 : (CM ? 4 : 5)) k_row(const StepP
 
     // Row items (group g, segment it) in steps of the warp count, advanced
     // without divisions: g += nw / nit, it += nw % nit with carry.
-    const int64_t nrows = P.n - P.row0;
+    const int64_t nrows = P.n - P.row0 - P.niso;
     const int64_t ng = (nrows + RW - 1) / RW;
     const int64_t dr = nw / nit;
     const int dit = (int)(nw - dr * nit);
@@ -608,8 +617,15 @@ __global__ void __launch_bounds__(256, BIG ? 6 : (CM ? 4 : 5)) k_row(const StepP
             const int32_t deg = e1 - e0;
             if (WM == W_UNIT) {
                 uint32_t lo = 0, hi = 0;
-                if (CM) count_bits<V, LR>(P, Scur + q, off, e0, deg, sl, lo, hi);
-                else count_unit<V, LR>(P, Scur + q, off, e0, deg, sl, lo, hi);
+                if (CM) {
+                    count_bits<V, LR>(P, Scur + q, off, e0, deg, sl, lo, hi);
+                } else if constexpr (BIG) {
+                    // one row per warp: the choice is warp-uniform
+                    if (deg >= P.bits_min) count_bits<V, LR>(P, Scur + q, off, e0, deg, sl, lo, hi);
+                    else count_unit<V, LR>(P, Scur + q, off, e0, deg, sl, lo, hi);
+                } else {
+                    count_unit<V, LR>(P, Scur + q, off, e0, deg, sl, lo, hi);
+                }
                 if constexpr (std::is_same<A, float>::value) {
                     // PRMT builds the float 2^23 + 2*count from a byte
                     // counter; minus (2^23 + deg) it is 2*count - deg exactly
@@ -743,10 +759,20 @@ __global__ void __launch_bounds__(256, BIG ? 6 : (CM ? 4 : 5)) k_row(const StepP
         const int64_t base = r * P.Ap + a0;
         uint32_t wp_old = 0;   // window steps: the previous window's word, fetched early
         if (WIN && (lane & (G - 1)) == 0) wp_old = P.Wp[r * P.W + q];
-        const RawT xr = vload_s<T, V>(xp + base, cs);
-        const RawT yr = vload_s<T, V>(yp + base, cs);
+        RawT xr, yr;
         A tv[V];
-        item_totals(r, q, off, tv);
+        bool wide = false;   // mixed mode: a bit-plane row (warp-uniform)
+        if constexpr (BIG && !CM && KIND != K_XY) wide = __ldg(&P.rowptr[r + 1]) - __ldg(&P.rowptr[r]) >= P.bits_min;
+        if (wide) {
+            // x, y fetched after the count: the planes need the registers
+            item_totals(r, q, off, tv);
+            xr = vload_s<T, V>(xp + base, cs);
+            yr = vload_s<T, V>(yp + base, cs);
+        } else {
+            xr = vload_s<T, V>(xp + base, cs);
+            yr = vload_s<T, V>(yp + base, cs);
+            item_totals(r, q, off, tv);
+        }
         finish(r, q, off, base, live, xr, yr, tv, row_c0(r), wp_old);
     }
     }
@@ -813,14 +839,17 @@ cudaError_t step_vl(const SolveDims &d, const DevCsr &J, const StepP &P, int off
     if (big) {
         Q.order = J.perm;
         Q.row0 = J.nheavy;
-    } else if (KIND != K_XY && (J.skewed || LR < 32)) {
+    } else if (KIND != K_XY && (J.skewed || LR < 32 || P.niso)) {
         Q.order = J.perm;
     }
-    const int64_t items = ((d.n - Q.row0 + RW - 1) / RW + (big ? J.nchunks : 0)) * nit;
-    // count mode of the +-1 rows: byte counters per lane (0) or bit planes (1);
-    // staged rows (x, y copied ahead into shared memory) for whole-warp rows
-    // of plain steps
-    const bool cm = d.tcm != 0;
+    // isolated rows (P.niso, left to k_iso) are the end of the degree order
+    if (P.niso && !Q.order) return cudaErrorInvalidValue;
+    const int64_t items = ((d.n - Q.row0 - P.niso + RW - 1) / RW + (big ? J.nchunks : 0)) * nit;
+    // count mode of the +-1 rows: byte counters per lane (0), bit planes (1),
+    // or mixed (2: the byte-counter kernel with P.bits_min set, heavy rows
+    // only); staged rows (x, y copied ahead into shared memory) for
+    // whole-warp rows of plain steps
+    const bool cm = d.tcm == 1;
     constexpr bool can_st = LR == 32 && !WIN && KIND != K_XY;
     const bool st = can_st && d.tst != 0 && J.unit;
     const size_t smem_st = (size_t)(bt / 32) * 4 * 32 * V * sizeof(T);
@@ -917,6 +946,106 @@ cudaError_t step_kw(const SolveDims &d, const DevCsr &J, const StepP &P, int off
         }
     }
     return cudaErrorInvalidValue;
+}
+
+// Isolated rows (degree 0, the last P.niso entries of P.order) have no
+// neighbour and are no row's neighbour: the force on them is zero at every
+// step and no step reads their signs.  One launch advances them through a
+// whole window of fused steps in registers -- each step the step kernel's
+// arithmetic (sb_update with a zero force) followed by the rounding to the
+// storage type that storing and reloading the state between launches does
+// -- and writes the signs of the window's last two steps to the planes the
+// step kernel would have written, with the window compare of its last
+// step.  The state it leaves is bit-identical to stepping the rows one
+// launch per step.  Thread: V agents of one row.
+template <class T, int V>
+__global__ void __launch_bounds__(256) k_iso(const StepP P, const int nsteps)
+{
+    using A = typename St<T>::A;
+    using RawT = Raw<V * sizeof(T)>;
+    extern __shared__ __align__(16) uint32_t s_chg[];
+    pdl_wait();
+    if (P.ctl[CTL_STOP]) return;   // grid-uniform
+    for (int q = threadIdx.x; q < P.W; q += blockDim.x) s_chg[q] = 0;
+    __syncthreads();
+    constexpr int G = 32 / V;   // lanes sharing one sign word
+    const int lane = threadIdx.x & 31;
+    const int step0 = P.ctl[CTL_STEP];
+    const int nseg = P.Ap / V;   // threads per row (a multiple of G)
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // lanes past the last row repeat it and store nothing (whole warps
+    // take part in the sign-word shuffles)
+    const bool live = t < P.niso * nseg;
+    const int64_t tt = live ? t : P.niso * nseg - 1;
+    const int64_t i = tt / nseg;
+    const int seg = (int)(tt - i * nseg);
+    const int64_t r = __ldg(&P.order[P.n - P.niso + i]);
+    const int a0 = seg * V, q = a0 >> 5, off = a0 & 31;
+    const int64_t base = r * P.Ap + a0;
+    T *xp = (T *)P.x, *yp = (T *)P.y;
+    const bool cs = P.stream_state != 0;
+    A x[V], y[V], zero[V];
+    {
+        const RawT xr = vload_s<T, V>(xp + base, cs), yr = vload_s<T, V>(yp + base, cs);
+        to_vals<T, V>(xr, x);
+        to_vals<T, V>(yr, y);
+    }
+#pragma unroll
+    for (int v = 0; v < V; v++) zero[v] = A(0);
+    A c0 = (A)P.c0;
+    if (P.c0r32) c0 = std::is_same<A, double>::value ? (A)__ldg(&P.c0r64[r]) : (A)__ldg(&P.c0r32[r]);
+    uint32_t bprev = 0, b = 0;
+    RawT xw, yw;
+    for (int k = 0; k < nsteps; k++) {
+        const auto c = Coef<A>::get(P, step0 + k);
+        sb_update<K_FUSED, false, V>(x, y, zero, c0, c, c);
+        xw = from_vals<T, V>(x);
+        yw = from_vals<T, V>(y);
+        to_vals<T, V>(xw, x);
+        to_vals<T, V>(yw, y);
+        bprev = b;
+        b = 0;
+#pragma unroll
+        for (int v = 0; v < V; v++) b |= sbit(x[v]) << v;
+    }
+    if (nsteps > 0 && live) {
+        vstore_s(xp + base, xw.u, cs);
+        vstore_s(yp + base, yw.u, cs);
+    }
+    b <<= off;
+    bprev <<= off;
+#pragma unroll
+    for (int sft = 1; sft < G; sft <<= 1) {
+        b |= __shfl_xor_sync(FULL, b, sft);
+        bprev |= __shfl_xor_sync(FULL, bprev, sft);
+    }
+    if (nsteps > 0 && live && (lane & (G - 1)) == 0) {
+        const int last = step0 + nsteps - 1;   // step k writes plane (k & 1) ^ 1
+        const int64_t wi = r * P.W + q;
+        ((last & 1) ? P.S0 : P.S1)[wi] = b;
+        if (nsteps > 1) ((last & 1) ? P.S1 : P.S0)[wi] = bprev;
+        // window compare of the last step, src/kernels.cu:37-46 + :84-90
+        const uint32_t ch = b ^ P.Wp[wi];
+        P.Wp[wi] = b;
+        if (ch) atomicOr(&s_chg[q], ch);
+    }
+    __syncthreads();
+    for (int qq = threadIdx.x; qq < P.W; qq += blockDim.x)
+        if (s_chg[qq]) atomicOr(&P.chg[qq], s_chg[qq]);
+    // late: the next step's CTAs would otherwise wait on SMs these need
+    pdl_trigger();
+}
+
+template <class T>
+cudaError_t iso_t(const SolveDims &d, const DevCsr &J, const StepP &P, cudaStream_t s)
+{
+    constexpr int V = 16 / (int)sizeof(T);
+    if (!P.niso || !P.order || d.Ap % 32) return cudaErrorInvalidValue;
+    const int64_t threads = P.niso * (d.Ap / V);
+    const int64_t blocks = (threads + 255) / 256;
+    if (blocks > INT32_MAX) return cudaErrorInvalidValue;
+    return launch(k_iso<T, V>, dim3((unsigned)blocks), dim3(256), sizeof(uint32_t) * d.W, s, d.pdl, P,
+                  (int)d.period);
 }
 
 template <class T>

@@ -10,4 +10,9 @@ cudaError_t step_bf16(const SolveDims &d, const DevCsr &J, const StepP &P, int k
     return step_t<__nv_bfloat16>(d, J, P, kind, win, offset, s);
 }
 
+cudaError_t iso_bf16(const SolveDims &d, const DevCsr &J, const StepP &P, cudaStream_t s)
+{
+    return iso_t<__nv_bfloat16>(d, J, P, s);
+}
+
 }  // namespace sbx

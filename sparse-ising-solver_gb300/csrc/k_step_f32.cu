@@ -10,4 +10,9 @@ cudaError_t step_f32(const SolveDims &d, const DevCsr &J, const StepP &P, int ki
     return step_t<float>(d, J, P, kind, win, offset, s);
 }
 
+cudaError_t iso_f32(const SolveDims &d, const DevCsr &J, const StepP &P, cudaStream_t s)
+{
+    return iso_t<float>(d, J, P, s);
+}
+
 }  // namespace sbx

@@ -10,4 +10,9 @@ cudaError_t step_f64(const SolveDims &d, const DevCsr &J, const StepP &P, int ki
     return step_t<double>(d, J, P, kind, win, offset, s);
 }
 
+cudaError_t iso_f64(const SolveDims &d, const DevCsr &J, const StepP &P, cudaStream_t s)
+{
+    return iso_t<double>(d, J, P, s);
+}
+
 }  // namespace sbx

@@ -165,6 +165,8 @@ StepP make_step(const SolveDims &d, const DevCsr &J, Work &w)
     P.part = (uint2 *)w.part;
     P.hcount = w.hcount;
     P.allpos = J.allpos ? 1 : 0;
+    P.bits_min = d.tcm == 2 ? kBitsMin : INT32_MAX;
+    P.niso = 0;
     P.nchunks = J.nchunks;
     P.order = nullptr;   // set per kernel (step_vl)
     P.row0 = 0;
@@ -198,6 +200,16 @@ cudaError_t step(const SolveDims &d, const DevCsr &J, const StepP &P, int kind, 
     }
 }
 
+cudaError_t iso(const SolveDims &d, const DevCsr &J, const StepP &P, cudaStream_t s)
+{
+    switch (d.prec) {
+    case P_F32: return iso_f32(d, J, P, s);
+    case P_BF16: return iso_bf16(d, J, P, s);
+    case P_F16: return iso_f16(d, J, P, s);
+    default: return iso_f64(d, J, P, s);
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_prestep(const SolveDims &d, const DevCsr &J, Work &w, cudaStream_t s,
@@ -215,6 +227,15 @@ cudaError_t launch_chunk(const SolveDims &d, const DevCsr &J, Work &w, cudaStrea
     cudaError_t e = cudaSuccess;
     if (!d.fused) {
         e = step(d, J, P, K_XY, false, 0, s);
+        *launches += 1;
+    } else if (J.niso) {
+        // isolated rows: the whole window in one launch; the step kernels
+        // skip them (events evs[2 * period], [2 * period + 1] in profile mode)
+        P.niso = J.niso;
+        P.order = J.perm;
+        if (evs) cudaEventRecord(evs[2 * d.period], s);
+        e = iso(d, J, P, s);
+        if (evs) cudaEventRecord(evs[2 * d.period + 1], s);
         *launches += 1;
     }
     for (int i = 0; i < d.period && e == cudaSuccess; i++) {

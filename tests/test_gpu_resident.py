@@ -43,6 +43,8 @@ CASES = [
     ("er3000", lambda: sbx.gen_er(3000, 0.004, pm1=True, seed=2), 40),
     ("rgg9000", lambda: sbx.gen_rgg(9000, 10.0, seed=3), 72),
     ("real1500", lambda: _real_graph(1500, 0.01, 4), 32),
+    # ~400 isolated rows: the streaming solve advances them a window per launch
+    ("er4000iso", lambda: sbx.gen_er(4000, 0.0006, pm1=True, seed=5), 64),
 ]
 
 

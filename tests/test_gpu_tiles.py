@@ -249,6 +249,53 @@ def test_dense_unit_rows_count_modes_bitexact_with_oracle(ctx, oracle, agents, c
     np.testing.assert_array_equal(y, oy)
 
 
+@pytest.mark.parametrize("count_mode", [1, 2, 3])
+def test_heavy_rows_count_modes_bitexact_with_oracle(ctx, oracle, count_mode):
+    # R-MAT: heavy rows (split into chunks), light rows on both sides of the
+    # mixed mode's degree threshold (12), and empty rows
+    g = sbx.gen_rmat(12, 8, seed=1234)
+    deg = np.diff(g.rowptr)
+    assert deg.max() > 127 and ((deg >= 12) & (deg <= 127)).sum() > 100 and ((deg > 0) & (deg < 12)).sum() > 100
+    A, max_steps, dt, seed = 64, 2000, 0.5, 9
+    prob = ctx.problem(g)
+    r, _ = ctx.solve(prob, sbx.params(dt=dt, steps=max_steps, run_steps=200, agents=A, fused=1,
+                                      seed=seed, precision=sbx.F64, kernel=sbx.KERNEL_STREAM,
+                                      count_mode=count_mode))
+    assert r["count_mode"] == count_mode
+    x, y, s = ctx.state(g.n, A)
+    og = oracle_graph(oracle, g)
+    ox, oy = oracle_first_steps(oracle, og, A, seed, dt, max_steps, 200, 1)
+    np.testing.assert_array_equal(x, ox)
+    np.testing.assert_array_equal(y, oy)
+
+
+@pytest.mark.parametrize("A,tile", [(64, (2, 32)), (32, (1, 32)), (32, (2, 16))])
+def test_isolated_rows_bitexact_with_oracle(ctx, oracle, A, tile):
+    # ~40 isolated rows (degree 0), advanced a window at a time by their own
+    # kernel, the others by the step kernel: FP64 state equal to the oracle's
+    g = sbx.gen_er(400, 0.006, pm1=True, seed=21)
+    assert (np.diff(g.rowptr) == 0).sum() > 20
+    max_steps, dt, seed = 2000, 0.5, 4
+    prob = ctx.problem(g)
+    ctx.solve(prob, sbx.params(dt=dt, steps=max_steps, run_steps=200, agents=A, fused=1, seed=seed,
+                               precision=sbx.F64, kernel=sbx.KERNEL_STREAM, lane_agents=tile[0],
+                               row_lanes=tile[1]))
+    x, y, s = ctx.state(g.n, A)
+    og = oracle_graph(oracle, g)
+    ox, oy = oracle_first_steps(oracle, og, A, seed, dt, max_steps, 200, 1)
+    np.testing.assert_array_equal(x, ox)
+    np.testing.assert_array_equal(y, oy)
+
+
+def test_mixed_count_mode_needs_heavy_rows(ctx):
+    g = sbx.gen_er(300, 0.05, pm1=True, seed=2)
+    prob = ctx.problem(g)
+    with pytest.raises(sbx.SbxError) as e:
+        ctx.solve(prob, sbx.params(dt=0.5, steps=100, agents=64, precision=sbx.BF16,
+                                   kernel=sbx.KERNEL_STREAM, count_mode=3))
+    assert e.value.rc == sbx.ERR_ARG
+
+
 @pytest.mark.parametrize("prec", [sbx.BF16, sbx.F32, sbx.F64])
 @pytest.mark.parametrize("count_mode", [1, 2])
 def test_staged_rows_give_the_same_state(ctx, prec, count_mode):
