@@ -413,7 +413,14 @@ def main():
     roof = None
     if rp["kernel_launches"] and rp["kernel_ms"] > 0:
         per_launch_s = rp["kernel_ms"] / 1000.0 / rp["kernel_launches"]
-        if rp["kernel_used"] == sbx.KERNEL_STREAM:
+        niso = int((inst.rowptr[1:] == inst.rowptr[:-1]).sum()) if wl["kind"] == "maxcut" else 0
+        if rp["kernel_used"] == sbx.KERNEL_STREAM and niso and wl["fused"]:
+            # isolated rows advance a window per k_iso launch (in registers):
+            # the unit is one SB step, its k_row launch plus 1/100 of k_iso
+            bytes_per_launch = b_step
+            kname = ("k_row + k_iso/100 (one SB step; %d isolated rows advanced a 100-step window "
+                     "per k_iso launch, effective bytes)" % niso)
+        elif rp["kernel_used"] == sbx.KERNEL_STREAM:
             bytes_per_launch, kname = b_step, "k_row (one SB step per launch)"
         else:
             # on-chip kernels run many steps per launch: B_step per step run

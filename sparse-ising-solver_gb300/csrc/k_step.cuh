@@ -957,94 +957,112 @@ cudaError_t step_kw(const SolveDims &d, const DevCsr &J, const StepP &P, int off
 // -- and writes the signs of the window's last two steps to the planes the
 // step kernel would have written, with the window compare of its last
 // step.  The state it leaves is bit-identical to stepping the rows one
-// launch per step.  Thread: V agents of one row.
-template <class T, int V>
-__global__ void __launch_bounds__(256) k_iso(const StepP P, const int nsteps)
+// launch per step.  Thread item: V agents of one row; warps stride over
+// groups of 32 items (warp-uniform trip counts for the sign shuffles).
+template <class T, int V, int NT>
+__global__ void __launch_bounds__(NT) k_iso(const StepP P, const int nsteps)
 {
     using A = typename St<T>::A;
     using RawT = Raw<V * sizeof(T)>;
     extern __shared__ __align__(16) uint32_t s_chg[];
     pdl_wait();
     if (P.ctl[CTL_STOP]) return;   // grid-uniform
-    for (int q = threadIdx.x; q < P.W; q += blockDim.x) s_chg[q] = 0;
+    for (int q = threadIdx.x; q < P.W; q += NT) s_chg[q] = 0;
     __syncthreads();
     constexpr int G = 32 / V;   // lanes sharing one sign word
     const int lane = threadIdx.x & 31;
     const int step0 = P.ctl[CTL_STEP];
-    const int nseg = P.Ap / V;   // threads per row (a multiple of G)
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    // lanes past the last row repeat it and store nothing (whole warps
-    // take part in the sign-word shuffles)
-    const bool live = t < P.niso * nseg;
-    const int64_t tt = live ? t : P.niso * nseg - 1;
-    const int64_t i = tt / nseg;
-    const int seg = (int)(tt - i * nseg);
-    const int64_t r = __ldg(&P.order[P.n - P.niso + i]);
-    const int a0 = seg * V, q = a0 >> 5, off = a0 & 31;
-    const int64_t base = r * P.Ap + a0;
+    const int nseg = P.Ap / V;   // items per row (a multiple of G)
+    const int64_t total = P.niso * nseg;
+    const int64_t nwarp = (int64_t)gridDim.x * (NT / 32);
     T *xp = (T *)P.x, *yp = (T *)P.y;
     const bool cs = P.stream_state != 0;
-    A x[V], y[V], zero[V];
-    {
-        const RawT xr = vload_s<T, V>(xp + base, cs), yr = vload_s<T, V>(yp + base, cs);
-        to_vals<T, V>(xr, x);
-        to_vals<T, V>(yr, y);
-    }
+    A zero[V];
 #pragma unroll
     for (int v = 0; v < V; v++) zero[v] = A(0);
-    A c0 = (A)P.c0;
-    if (P.c0r32) c0 = std::is_same<A, double>::value ? (A)__ldg(&P.c0r64[r]) : (A)__ldg(&P.c0r32[r]);
-    uint32_t bprev = 0, b = 0;
-    RawT xw, yw;
-    for (int k = 0; k < nsteps; k++) {
-        const auto c = Coef<A>::get(P, step0 + k);
-        sb_update<K_FUSED, false, V>(x, y, zero, c0, c, c);
-        xw = from_vals<T, V>(x);
-        yw = from_vals<T, V>(y);
+    const int last = step0 + nsteps - 1;   // step k writes plane (k & 1) ^ 1
+    uint32_t *Sl = (last & 1) ? P.S0 : P.S1, *Sp = (last & 1) ? P.S1 : P.S0;
+    for (int64_t wg = (int64_t)blockIdx.x * (NT / 32) + (threadIdx.x >> 5); wg * 32 < total; wg += nwarp) {
+        // lanes past the last item repeat it and store nothing
+        const int64_t t = wg * 32 + lane;
+        const bool live = t < total;
+        const int64_t tt = live ? t : total - 1;
+        const int64_t i = tt / nseg;
+        const int seg = (int)(tt - i * nseg);
+        const int64_t r = __ldg(&P.order[P.n - P.niso + i]);
+        const int a0 = seg * V, q = a0 >> 5, off = a0 & 31;
+        const int64_t base = r * P.Ap + a0;
+        A x[V], y[V];
+        RawT xw = vload_s<T, V>(xp + base, cs), yw = vload_s<T, V>(yp + base, cs);
         to_vals<T, V>(xw, x);
         to_vals<T, V>(yw, y);
-        bprev = b;
-        b = 0;
+        A c0 = (A)P.c0;
+        if (P.c0r32) c0 = std::is_same<A, double>::value ? (A)__ldg(&P.c0r64[r]) : (A)__ldg(&P.c0r32[r]);
+        auto one = [&](int k) {
+            const auto c = Coef<A>::get(P, step0 + k);
+            sb_update<K_FUSED, false, V>(x, y, zero, c0, c, c);
+            xw = from_vals<T, V>(x);
+            yw = from_vals<T, V>(y);
+            to_vals<T, V>(xw, x);
+            to_vals<T, V>(yw, y);
+        };
+        auto signs = [&]() {
+            uint32_t b = 0;
 #pragma unroll
-        for (int v = 0; v < V; v++) b |= sbit(x[v]) << v;
-    }
-    if (nsteps > 0 && live) {
-        vstore_s(xp + base, xw.u, cs);
-        vstore_s(yp + base, yw.u, cs);
-    }
-    b <<= off;
-    bprev <<= off;
+            for (int v = 0; v < V; v++) b |= sbit(x[v]) << v;
+            return b << off;
+        };
+        const int body = nsteps > 2 ? nsteps - 2 : 0;
+#pragma unroll 1
+        for (int k = 0; k < body; k++) one(k);
+        uint32_t bprev = 0, b = 0;
+        for (int k = body; k < nsteps; k++) {
+            one(k);
+            bprev = b;
+            b = signs();
+        }
+        if (nsteps > 0 && live) {
+            vstore_s(xp + base, xw.u, cs);
+            vstore_s(yp + base, yw.u, cs);
+        }
 #pragma unroll
-    for (int sft = 1; sft < G; sft <<= 1) {
-        b |= __shfl_xor_sync(FULL, b, sft);
-        bprev |= __shfl_xor_sync(FULL, bprev, sft);
-    }
-    if (nsteps > 0 && live && (lane & (G - 1)) == 0) {
-        const int last = step0 + nsteps - 1;   // step k writes plane (k & 1) ^ 1
-        const int64_t wi = r * P.W + q;
-        ((last & 1) ? P.S0 : P.S1)[wi] = b;
-        if (nsteps > 1) ((last & 1) ? P.S1 : P.S0)[wi] = bprev;
-        // window compare of the last step, src/kernels.cu:37-46 + :84-90
-        const uint32_t ch = b ^ P.Wp[wi];
-        P.Wp[wi] = b;
-        if (ch) atomicOr(&s_chg[q], ch);
+        for (int sft = 1; sft < G; sft <<= 1) {
+            b |= __shfl_xor_sync(FULL, b, sft);
+            bprev |= __shfl_xor_sync(FULL, bprev, sft);
+        }
+        if (nsteps > 0 && live && (lane & (G - 1)) == 0) {
+            const int64_t wi = r * P.W + q;
+            Sl[wi] = b;
+            if (nsteps > 1) Sp[wi] = bprev;
+            // window compare of the last step, src/kernels.cu:37-46 + :84-90
+            const uint32_t ch = b ^ P.Wp[wi];
+            P.Wp[wi] = b;
+            if (ch) atomicOr(&s_chg[q], ch);
+        }
     }
     __syncthreads();
-    for (int qq = threadIdx.x; qq < P.W; qq += blockDim.x)
+    for (int qq = threadIdx.x; qq < P.W; qq += NT)
         if (s_chg[qq]) atomicOr(&P.chg[qq], s_chg[qq]);
     // late: the next step's CTAs would otherwise wait on SMs these need
     pdl_trigger();
 }
 
+// 256-thread blocks, each warp four groups of 32 items.
 template <class T>
 cudaError_t iso_t(const SolveDims &d, const DevCsr &J, const StepP &P, cudaStream_t s)
 {
     constexpr int V = 16 / (int)sizeof(T);
     if (!P.niso || !P.order || d.Ap % 32) return cudaErrorInvalidValue;
-    const int64_t threads = P.niso * (d.Ap / V);
-    const int64_t blocks = (threads + 255) / 256;
-    if (blocks > INT32_MAX) return cudaErrorInvalidValue;
-    return launch(k_iso<T, V>, dim3((unsigned)blocks), dim3(256), sizeof(uint32_t) * d.W, s, d.pdl, P,
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    }
+    const size_t smem = sizeof(uint32_t) * d.W;
+    const int64_t warps = (P.niso * (d.Ap / V) + 31) / 32;
+    const int64_t blocks = std::min<int64_t>((warps + 4 * 8 - 1) / (4 * 8), (int64_t)nsm * 64);
+    return launch(k_iso<T, V, 256>, dim3((unsigned)std::max<int64_t>(blocks, 1)), dim3(256), smem, s, d.pdl, P,
                   (int)d.period);
 }
 

@@ -229,8 +229,10 @@ cudaError_t launch_chunk(const SolveDims &d, const DevCsr &J, Work &w, cudaStrea
         e = step(d, J, P, K_XY, false, 0, s);
         *launches += 1;
     } else if (J.niso) {
-        // isolated rows: the whole window in one launch; the step kernels
-        // skip them (events evs[2 * period], [2 * period + 1] in profile mode)
+        // isolated rows: the whole window in one launch, which the step
+        // kernels skip (events evs[2 * period], [2 * period + 1] in profile
+        // mode).  Run beside the step kernels on a second stream it was
+        // slower: they take the SMs' issue slots and registers.
         P.niso = J.niso;
         P.order = J.perm;
         if (evs) cudaEventRecord(evs[2 * d.period], s);

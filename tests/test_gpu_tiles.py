@@ -269,17 +269,19 @@ def test_heavy_rows_count_modes_bitexact_with_oracle(ctx, oracle, count_mode):
     np.testing.assert_array_equal(y, oy)
 
 
+@pytest.mark.parametrize("count_mode", [1, 2])
 @pytest.mark.parametrize("A,tile", [(64, (2, 32)), (32, (1, 32)), (32, (2, 16))])
-def test_isolated_rows_bitexact_with_oracle(ctx, oracle, A, tile):
+def test_isolated_rows_bitexact_with_oracle(ctx, oracle, A, tile, count_mode):
     # ~40 isolated rows (degree 0), advanced a window at a time by their own
-    # kernel, the others by the step kernel: FP64 state equal to the oracle's
+    # kernel, the others by the step kernel (byte counters or bit planes):
+    # FP64 state equal to the oracle's
     g = sbx.gen_er(400, 0.006, pm1=True, seed=21)
     assert (np.diff(g.rowptr) == 0).sum() > 20
     max_steps, dt, seed = 2000, 0.5, 4
     prob = ctx.problem(g)
     ctx.solve(prob, sbx.params(dt=dt, steps=max_steps, run_steps=200, agents=A, fused=1, seed=seed,
                                precision=sbx.F64, kernel=sbx.KERNEL_STREAM, lane_agents=tile[0],
-                               row_lanes=tile[1]))
+                               row_lanes=tile[1], count_mode=count_mode))
     x, y, s = ctx.state(g.n, A)
     og = oracle_graph(oracle, g)
     ox, oy = oracle_first_steps(oracle, og, A, seed, dt, max_steps, 200, 1)
