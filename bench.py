@@ -61,7 +61,8 @@ PBYTES = {"f32": 4, "bf16": 2, "f16": 2, "f64": 8}
 # tile the bench runs; the resident kernels' launch covers the whole solve).
 TRAFFIC = {
     "torus": (45.85e6, "profiles/k_resident_rs_bf16_torus100x100.md (20,000-step launch)"),
-    "rmat20": (2.2139e9, "profiles/k_row_bf16_rmat20.md"),
+    # per SB step: the k_row launch plus 1/100 of the isolated rows' k_iso
+    "rmat20": (9.886e8, "profiles/k_row_bf16_rmat20.md (k_row launch + k_iso/100)"),
     "batch512": (1.3393e9, "profiles/k_row_bf16_batch512.md"),
 }
 
@@ -470,7 +471,7 @@ def main():
             "quality": qual,
             "time_to_target": ttt,
             "tile": {k: r_main[k] for k in ("lane_agents", "row_lanes", "block_threads",
-                                            "agents_per_block")},
+                                            "count_mode", "staging", "agents_per_block")},
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -630,7 +631,8 @@ def run_batch(args, wl, rank, world, local):
                         "within_0.1pct_of_fp32_plain": float(np.mean(rel <= 1e-3)),
                         "mean_rel_gap": float(np.mean(rel)), "max_rel_gap": float(np.max(rel))},
             "time_to_target": ttt,
-            "tile": {k: res[0][k] for k in ("lane_agents", "row_lanes", "block_threads")},
+            "tile": {k: res[0][k] for k in ("lane_agents", "row_lanes", "block_threads", "count_mode",
+                                            "staging")},
         }
         print(json.dumps(line), flush=True)
     ctx.close()
