@@ -226,6 +226,14 @@ __device__ __forceinline__ uint32_t plane_ld(const uint32_t *Sq, uint32_t col, i
     return __ldg((const uint32_t *)((const char *)Sq + (uint64_t)col * (uint64_t)wb));
 }
 
+// Full adder over 32 bit lanes: a + b + e -> sum into a, carry returned.
+__device__ __forceinline__ uint32_t fadd(uint32_t &a, uint32_t b, uint32_t e)
+{
+    const uint32_t c = (a & b) | (e & (a ^ b));
+    a = a ^ b ^ e;
+    return c;
+}
+
 // Twice the sign bits of a nibble, one per byte: byte i of the result is
 // 2 * bit i.  Byte counters of +-1 neighbours then hold 2 * count (<= 254 for
 // up to kHeavy = 127 neighbours).
@@ -321,25 +329,53 @@ __device__ __forceinline__ void count_bits_s(const StepP &P, const uint32_t *Sq,
                 }
             }
         }
-        // pairs of words through a full adder into plane 0, the carry
-        // rippling up the planes
+        static_assert(T * KPL == V, "V words per lane per block");
+        if constexpr (V >= 4) {
+            // carry-save tree: the block's V words (zero past the rows'
+            // ends) meet the planes in full adders, level by level, and
+            // only the top carry ripples
+            uint32_t c2[V / 4], c4;
 #pragma unroll
-        for (int i = 0; i < T * KPL; i += 2) {
-            if (cb + (i / KPL) * LR >= dmax) break;   // warp-uniform
-            uint32_t c;
-            if (i + 1 < T * KPL) {
-                const uint32_t a = p[0], b = w[i], e = w[i + 1];
-                p[0] = a ^ b ^ e;
-                c = (a & b) | (e & (a ^ b));
+            for (int h = 0; h < V / 4; h++) {
+                uint32_t c1[2];
+#pragma unroll
+                for (int i = 0; i < 2; i++)
+                    c1[i] = fadd(p[0], w[4 * h + 2 * i], w[4 * h + 2 * i + 1]);
+                c2[h] = fadd(p[1], c1[0], c1[1]);
+            }
+            int k0;
+            if constexpr (V == 8) {
+                c4 = fadd(p[2], c2[0], c2[1]);
+                k0 = 3;
             } else {
-                c = p[0] & w[i];
-                p[0] ^= w[i];
+                c4 = c2[0];
+                k0 = 2;
             }
 #pragma unroll
-            for (int k = 1; k < BL; k++) {
-                const uint32_t t = p[k] & c;
-                p[k] ^= c;
-                c = t;
+            for (int k = k0; k < BL; k++) {
+                const uint32_t t = p[k] & c4;
+                p[k] ^= c4;
+                c4 = t;
+            }
+        } else {
+            // pairs of words through a full adder into plane 0, the carry
+            // rippling up the planes
+#pragma unroll
+            for (int i = 0; i < T * KPL; i += 2) {
+                if (cb + (i / KPL) * LR >= dmax) break;   // warp-uniform
+                uint32_t c;
+                if (i + 1 < T * KPL) {
+                    c = fadd(p[0], w[i], w[i + 1]);
+                } else {
+                    c = p[0] & w[i];
+                    p[0] ^= w[i];
+                }
+#pragma unroll
+                for (int k = 1; k < BL; k++) {
+                    const uint32_t t = p[k] & c;
+                    p[k] ^= c;
+                    c = t;
+                }
             }
         }
     }
