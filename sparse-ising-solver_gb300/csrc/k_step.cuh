@@ -777,24 +777,26 @@ __global__ void __launch_bounds__(256, BIG ? 6 : (CM ? 4 : 5)) k_row(const StepP
             j++;
         }
     } else {
-    int64_t g = w0 / nit;
-    int it = (int)(w0 - g * nit);
-    for (; g < ng; g += dr, it += dit) {
+    // 32-bit row arithmetic (rows < 2^31); 64-bit only for state offsets
+    const int32_t nr32 = (int32_t)nrows, ng32 = (int32_t)ng, dr32 = (int32_t)dr, row0 = (int32_t)P.row0;
+    int32_t g = (int32_t)(w0 / nit);
+    int it = (int)(w0 - (int64_t)g * nit);
+    for (; g < ng32; g += dr32, it += dit) {
         if (it >= nit) {
             it -= nit;
             g++;
-            if (g >= ng) break;
+            if (g >= ng32) break;
         }
         // lanes of a group past the last row repeat the last row, store nothing
-        const int64_t gi = g * RW + rw;
-        const bool live = RW == 1 || gi < nrows;
-        const int64_t ri = P.row0 + (live ? gi : nrows - 1);
-        const int64_t r = P.order ? (int64_t)__ldg(&P.order[ri]) : ri;
+        const int32_t gi = g * RW + rw;
+        const bool live = RW == 1 || gi < nr32;
+        const int32_t ri = row0 + (live ? gi : nr32 - 1);
+        const int32_t r = P.order ? __ldg(&P.order[ri]) : ri;
         const int a0 = it * LR * V + sl * V;
         const int q = a0 >> 5, off = a0 & 31;
-        const int64_t base = r * P.Ap + a0;
+        const int64_t base = (int64_t)r * P.Ap + a0;
         uint32_t wp_old = 0;   // window steps: the previous window's word, fetched early
-        if (WIN && (lane & (G - 1)) == 0) wp_old = P.Wp[r * P.W + q];
+        if (WIN && (lane & (G - 1)) == 0) wp_old = P.Wp[(int64_t)r * P.W + q];
         RawT xr, yr;
         A tv[V];
         bool wide = false;   // mixed mode: a bit-plane row (warp-uniform)
