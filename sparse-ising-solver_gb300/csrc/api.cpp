@@ -295,10 +295,13 @@ int ensure_common(sbx_ctx *ctx, const SolveDims &d, int64_t total_steps, int32_t
     const size_t es = prec_bytes(d.prec);
     const size_t nst = (size_t)d.n * d.Ap;
     const size_t npl = (size_t)d.n * d.W;
+    // sign planes: one extra row (n), always zero, that the step kernels
+    // read for neighbours past a row's end
+    const size_t nsp = npl + (size_t)d.W;
     CK(growv(w.x, w.cap_x, nst * es));
     CK(growv(w.y, w.cap_y, nst * es));
-    CK(grow(w.S[0], w.cap_S0, npl));
-    CK(grow(w.S[1], w.cap_S1, npl));
+    CK(grow(w.S[0], w.cap_S0, nsp));
+    CK(grow(w.S[1], w.cap_S1, nsp));
     CK(grow(w.Wp, w.cap_Wp, npl));
     CK(grow(w.fin, w.cap_fin, npl));
     CK(grow(w.chg, w.cap_chg, (size_t)d.W));
@@ -324,8 +327,8 @@ int ensure_common(sbx_ctx *ctx, const SolveDims &d, int64_t total_steps, int32_t
     cudaStream_t s = ctx->stream;
     CK(cudaMemsetAsync(w.Wp, 0xff, npl * 4, s));   // current_spins = -1 (ising.cu:128)
     CK(cudaMemsetAsync(w.fin, 0xff, npl * 4, s));  // final_spins = -1 (ising.cu:129)
-    CK(cudaMemsetAsync(w.S[0], 0, npl * 4, s));
-    CK(cudaMemsetAsync(w.S[1], 0, npl * 4, s));
+    CK(cudaMemsetAsync(w.S[0], 0, nsp * 4, s));
+    CK(cudaMemsetAsync(w.S[1], 0, nsp * 4, s));
     CK(cudaMemsetAsync(w.chg, 0, (size_t)d.W * 4, s));
     CK(cudaMemsetAsync(w.newmask, 0, (size_t)d.W * 4, s));
     CK(cudaMemsetAsync(w.stab, 0, (size_t)d.Ap * 4, s));

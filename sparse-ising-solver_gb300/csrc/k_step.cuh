@@ -48,6 +48,7 @@ struct StepP {
     const double *__restrict__ c0r64;
     int64_t n;
     int32_t W, Ap, nchunks;
+    uint32_t zrow;                        // n: the sign planes' all-zero row (column of no neighbour)
     int32_t stream_state;                 // state larger than L2: x, y loads/stores evict first
     int32_t allpos;                       // every weight is +1: no sign bits in colw
     int32_t bits_min;                     // heavy-row kernels: light rows of this degree or more
@@ -253,20 +254,19 @@ __device__ __forceinline__ void count_unit_s(const StepP &P, const uint32_t *Sq,
     for (int32_t cb = 0; cb < dmax; cb += LR) {
         const int m = min(LR, dmax - cb);
         const int32_t idx = cb + sl;
-        const uint32_t mycw = idx < dw ? __ldg(&P.colw[e0 + idx]) : 0u;
+        // past the row's end: the all-zero row, whose terms vanish
+        const uint32_t mycw = idx < dw ? __ldg(&P.colw[e0 + idx]) : P.zrow;
 #pragma unroll 4
         for (int k = 0; k < m; k++) {
             const uint32_t cw = __shfl_sync(FULL, mycw, k, LR);
-            if (LR == 32 || cb + k < dw) {
-                // all weights +1: bit 31 is clear, no sign to apply
-                const uint32_t word = plane_ld(Sq, NEG ? (cw & 0x7fffffffu) : cw, P.W);
-                // weight sign -> all-ones mask; unused high bits only reach
-                // counter bytes that are never read
-                uint32_t bits = word >> off;
-                if (NEG) bits ^= (uint32_t)((int32_t)cw >> 31);
-                lo += spread2x(bits & 0xfu);
-                if (V == 8) hi += spread2x((bits >> 4) & 0xfu);
-            }
+            // all weights +1: bit 31 is clear, no sign to apply
+            const uint32_t word = plane_ld(Sq, NEG ? (cw & 0x7fffffffu) : cw, P.W);
+            // weight sign -> all-ones mask; unused high bits only reach
+            // counter bytes that are never read
+            uint32_t bits = word >> off;
+            if (NEG) bits ^= (uint32_t)((int32_t)cw >> 31);
+            lo += spread2x(bits & 0xfu);
+            if (V == 8) hi += spread2x((bits >> 4) & 0xfu);
         }
     }
 }
@@ -308,11 +308,13 @@ __device__ __forceinline__ void count_bits_s(const StepP &P, const uint32_t *Sq,
     constexpr int T = 32 / LR;     // column words per lane per block
     constexpr int KPL = LR / G;    // neighbours per lane per column word
     for (int32_t cb = 0; cb < dmax; cb += 32) {
+        // past a row's end: the zero row (word 0, weight sign clear), so
+        // those terms vanish without a test per word
         uint32_t mycw[T];
 #pragma unroll
         for (int t = 0; t < T; t++) {
             const int32_t idx = cb + t * LR + sl;
-            mycw[t] = idx < dw ? __ldg(&P.colw[e0 + idx]) : 0u;
+            mycw[t] = idx < dw ? __ldg(&P.colw[e0 + idx]) : P.zrow;
         }
         uint32_t w[T * KPL];
 #pragma unroll
@@ -323,9 +325,8 @@ __device__ __forceinline__ void count_bits_s(const StepP &P, const uint32_t *Sq,
                 const uint32_t cw = __shfl_sync(FULL, mycw[t], src, LR);
                 w[t * KPL + kk] = 0u;
                 if (cb + t * LR < dmax) {
-                    // past the row's end cw is 0: row 0 is read, the term dropped
                     const uint32_t word = plane_ld(Sq, NEG ? (cw & 0x7fffffffu) : cw, P.W);
-                    w[t * KPL + kk] = (cb + t * LR + src < dw) ? (NEG ? word ^ (uint32_t)((int32_t)cw >> 31) : word) : 0u;
+                    w[t * KPL + kk] = NEG ? word ^ (uint32_t)((int32_t)cw >> 31) : word;
                 }
             }
         }

@@ -173,6 +173,7 @@ StepP make_step(const SolveDims &d, const DevCsr &J, Work &w)
     P.c0r32 = J.c0r32;
     P.c0r64 = J.c0r64;
     P.n = d.n;
+    P.zrow = (uint32_t)d.n;
     P.W = d.W;
     {
         static int l2 = -1;
