@@ -251,11 +251,12 @@ __device__ __forceinline__ void count_unit_s(const StepP &P, const uint32_t *Sq,
 {
     int32_t dmax = dw;
     if constexpr (LR < 32) dmax = __reduce_max_sync(FULL, dw);
+    const uint32_t *cwp = P.colw + e0 + sl;   // this lane's column words, from one base
     for (int32_t cb = 0; cb < dmax; cb += LR) {
         const int m = min(LR, dmax - cb);
         const int32_t idx = cb + sl;
         // past the row's end: the all-zero row, whose terms vanish
-        const uint32_t mycw = idx < dw ? __ldg(&P.colw[e0 + idx]) : P.zrow;
+        const uint32_t mycw = idx < dw ? __ldg(cwp + cb) : P.zrow;
 #pragma unroll 4
         for (int k = 0; k < m; k++) {
             const uint32_t cw = __shfl_sync(FULL, mycw, k, LR);
@@ -307,6 +308,7 @@ __device__ __forceinline__ void count_bits_s(const StepP &P, const uint32_t *Sq,
     // warp are skipped (warp-uniform).
     constexpr int T = 32 / LR;     // column words per lane per block
     constexpr int KPL = LR / G;    // neighbours per lane per column word
+    const uint32_t *cwp = P.colw + e0 + sl;   // this lane's column words, from one base
     for (int32_t cb = 0; cb < dmax; cb += 32) {
         // past a row's end: the zero row (word 0, weight sign clear), so
         // those terms vanish without a test per word
@@ -314,7 +316,7 @@ __device__ __forceinline__ void count_bits_s(const StepP &P, const uint32_t *Sq,
 #pragma unroll
         for (int t = 0; t < T; t++) {
             const int32_t idx = cb + t * LR + sl;
-            mycw[t] = idx < dw ? __ldg(&P.colw[e0 + idx]) : P.zrow;
+            mycw[t] = idx < dw ? __ldg(cwp + cb + t * LR) : P.zrow;
         }
         uint32_t w[T * KPL];
 #pragma unroll
