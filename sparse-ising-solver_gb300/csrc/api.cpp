@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "host_par.h"
 
 using namespace sbx;
 
@@ -164,67 +165,123 @@ void free_csr(DevCsr &J)
 
 // Upload a validated CSR; classify its weights.
 int upload_csr(sbx_ctx *ctx, DevCsr &J, int64_t n, int64_t nnz, const int32_t *rowptr,
-               const int32_t *col, const double *val, double wsum)
+               const int32_t *col, const double *val, double wsum, bool weights_always = false)
 {
     if (n <= 0 || n > INT32_MAX - 1 || nnz < 0 || nnz > INT32_MAX || !rowptr || (nnz && (!col || !val)))
         return fail(ctx, SBX_ERR_ARG, "bad CSR sizes or pointers");
     if (rowptr[0] != 0 || rowptr[n] != nnz) return fail(ctx, SBX_ERR_ARG, "rowptr[0] != 0 or rowptr[n] != nnz");
-    int32_t maxdeg = 0;
-    for (int64_t r = 0; r < n; r++) {
-        if (rowptr[r + 1] < rowptr[r]) return fail(ctx, SBX_ERR_ARG, "rowptr not monotone");
-        maxdeg = std::max(maxdeg, rowptr[r + 1] - rowptr[r]);
-    }
-    bool unit = true, integer = true;
-    double rowabs_max = 0;
-    std::vector<uint32_t> colw((size_t)nnz);
-    std::vector<float> valf((size_t)nnz);
-    for (int64_t r = 0; r < n; r++) {
-        double ra = 0;
-        for (int32_t e = rowptr[r]; e < rowptr[r + 1]; e++) {
-            if (col[e] < 0 || col[e] >= n) return fail(ctx, SBX_ERR_ARG, "column index out of range");
-            const double v = val[e];
-            if (!std::isfinite(v)) return fail(ctx, SBX_ERR_ARG, "non-finite weight");
-            if (std::fabs(v) != 1.0) unit = false;
-            if (v != std::floor(v) || std::fabs(v) > 16777216.0) integer = false;
-            ra += std::fabs(v);
-            valf[e] = (float)v;
+    // Checks and classification on host threads over row ranges (large
+    // matrices); each range keeps its own flags, merged after.
+    const int T = nnz > (1 << 20) ? host_threads() : 1;
+    struct Part {
+        int err = 0;   // 1 rowptr, 2 column, 3 weight
+        int32_t maxdeg = 0;
+        int64_t niso = 0;
+        bool unit = true, integer = true, neg = false;
+        double rowabs = 0;
+    };
+    std::vector<Part> part((size_t)T);
+    parallel(T, [&](int t, int TT) {
+        Part &a = part[(size_t)t];
+        const int64_t r0 = n * t / TT, r1 = n * (t + 1) / TT;
+        for (int64_t r = r0; r < r1; r++) {
+            const int32_t deg = rowptr[r + 1] - rowptr[r];
+            if (deg < 0) {
+                a.err = 1;
+                return;
+            }
+            a.maxdeg = std::max(a.maxdeg, deg);
+            a.niso += deg == 0;
         }
-        rowabs_max = std::max(rowabs_max, ra);
+    });
+    for (const Part &a : part)
+        if (a.err) return fail(ctx, SBX_ERR_ARG, "rowptr not monotone");
+    parallel(T, [&](int t, int TT) {
+        Part &a = part[(size_t)t];
+        const int64_t r0 = n * t / TT, r1 = n * (t + 1) / TT;
+        for (int64_t r = r0; r < r1 && !a.err; r++) {
+            double ra = 0;
+            for (int32_t e = rowptr[r]; e < rowptr[r + 1]; e++) {
+                if (col[e] < 0 || col[e] >= n) {
+                    a.err = 2;
+                    break;
+                }
+                const double v = val[e];
+                if (!std::isfinite(v)) {
+                    a.err = 3;
+                    break;
+                }
+                if (std::fabs(v) != 1.0) a.unit = false;
+                if (v != std::floor(v) || std::fabs(v) > 16777216.0) a.integer = false;
+                a.neg |= v < 0;
+                ra += std::fabs(v);
+            }
+            a.rowabs = std::max(a.rowabs, ra);
+        }
+    });
+    int32_t maxdeg = 0;
+    int64_t niso = 0;
+    bool unit = true, integer = true, neg = false;
+    double rowabs_max = 0;
+    for (const Part &a : part) {
+        if (a.err == 2) return fail(ctx, SBX_ERR_ARG, "column index out of range");
+        if (a.err == 3) return fail(ctx, SBX_ERR_ARG, "non-finite weight");
+        maxdeg = std::max(maxdeg, a.maxdeg);
+        niso += a.niso;
+        unit &= a.unit;
+        integer &= a.integer;
+        neg |= a.neg;
+        rowabs_max = std::max(rowabs_max, a.rowabs);
     }
     if (rowabs_max >= 2147483647.0) integer = false;
-    for (int64_t e = 0; e < nnz; e++)
-        colw[e] = (uint32_t)col[e] | ((unit && val[e] < 0) ? 0x80000000u : 0u);
-    // rows by decreasing degree: a warp of the resident kernel gets rows of
-    // similar length
-    std::vector<int32_t> perm((size_t)n);
-    std::iota(perm.begin(), perm.end(), 0);
-    std::stable_sort(perm.begin(), perm.end(), [&](int32_t a, int32_t b) {
-        return rowptr[a + 1] - rowptr[a] > rowptr[b + 1] - rowptr[b];
+    // column words (bit 31: a -1 weight); FP32 weights for other matrices
+    std::vector<uint32_t> colw((size_t)nnz);
+    const bool dev_weights = !unit || weights_always;
+    std::vector<float> valf(dev_weights ? (size_t)nnz : 0);
+    parallel(T, [&](int t, int TT) {
+        const int64_t e0 = nnz * t / TT, e1 = nnz * (t + 1) / TT;
+        for (int64_t e = e0; e < e1; e++) {
+            colw[e] = (uint32_t)col[e] | ((unit && val[e] < 0) ? 0x80000000u : 0u);
+            if (dev_weights) valf[e] = (float)val[e];
+        }
     });
+    // rows by decreasing degree, ties in row order (a counting sort): a warp
+    // of the resident kernel gets rows of similar length
+    std::vector<int32_t> perm((size_t)n);
+    {
+        std::vector<int64_t> at((size_t)maxdeg + 2, 0);
+        for (int64_t r = 0; r < n; r++) at[(size_t)(maxdeg - (rowptr[r + 1] - rowptr[r])) + 1]++;
+        for (int32_t k = 0; k <= maxdeg; k++) at[(size_t)k + 1] += at[(size_t)k];
+        for (int64_t r = 0; r < n; r++) perm[(size_t)at[(size_t)(maxdeg - (rowptr[r + 1] - rowptr[r]))]++] = (int32_t)r;
+    }
     J.n = n;
     J.nnz = nnz;
     J.unit = unit;
-    J.allpos = unit && std::all_of(val, val + nnz, [](double v) { return v > 0; });
+    J.allpos = unit && !neg;
     J.integer = integer;
     J.wsum = wsum;
     J.max_deg = maxdeg;
     J.skewed = (double)maxdeg > 8.0 * std::max(1.0, (double)nnz / (double)n);
-    J.niso = 0;
-    for (int64_t r = 0; r < n; r++) J.niso += rowptr[r + 1] == rowptr[r];
+    J.niso = niso;
     J.hval.assign(val, val + nnz);
     J.hrowptr.assign(rowptr, rowptr + n + 1);
     J.hcol.assign(col, col + nnz);
     J.hperm = perm;
     CK(cudaMalloc(&J.rowptr, sizeof(int32_t) * (n + 1)));
     CK(cudaMalloc(&J.colw, sizeof(uint32_t) * std::max<int64_t>(nnz, 1)));
-    CK(cudaMalloc(&J.vald, sizeof(double) * std::max<int64_t>(nnz, 1)));
-    CK(cudaMalloc(&J.valf, sizeof(float) * std::max<int64_t>(nnz, 1)));
     CK(cudaMalloc(&J.perm, sizeof(int32_t) * n));
     CK(cudaMemcpy(J.rowptr, rowptr, sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice));
-    if (nnz) {
-        CK(cudaMemcpy(J.colw, colw.data(), sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(J.vald, val, sizeof(double) * nnz, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(J.valf, valf.data(), sizeof(float) * nnz, cudaMemcpyHostToDevice));
+    if (nnz) CK(cudaMemcpy(J.colw, colw.data(), sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice));
+    // weights on the device only when they are not all +-1 (the MaxCut
+    // kernels read the sign bit of colw for +-1 matrices), or when asked (the
+    // TSP QUBO's kernels always read them)
+    if (dev_weights) {
+        CK(cudaMalloc(&J.vald, sizeof(double) * std::max<int64_t>(nnz, 1)));
+        CK(cudaMalloc(&J.valf, sizeof(float) * std::max<int64_t>(nnz, 1)));
+        if (nnz) {
+            CK(cudaMemcpy(J.vald, val, sizeof(double) * nnz, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(J.valf, valf.data(), sizeof(float) * nnz, cudaMemcpyHostToDevice));
+        }
     }
     CK(cudaMemcpy(J.perm, perm.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
     if (unit && maxdeg > kHeavy) {
@@ -1569,7 +1626,7 @@ int sbx_problem_tsp(sbx_ctx *ctx, int32_t N, const double *packed, double A, dou
                     }
                 rp[(size_t)i * N + k + 1] = (int32_t)col.size();
             }
-        rc = upload_csr(ctx, t.qubo, m, (int64_t)col.size(), rp.data(), col.data(), val.data(), 0.0);
+        rc = upload_csr(ctx, t.qubo, m, (int64_t)col.size(), rp.data(), col.data(), val.data(), 0.0, true);
     }
     if (rc) {
         cudaFree(t.D);

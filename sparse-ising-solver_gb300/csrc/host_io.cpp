@@ -9,6 +9,7 @@
 // keeps empty rows (src/csr.cpp:168-186 drops their row pointer) and returns
 // an error where the reference loops forever on a missing or malformed file.
 #include "../../include/sbx.h"
+#include "host_par.h"
 
 #include <algorithm>
 #include <cmath>
@@ -87,25 +88,8 @@ struct Entry {
     double v;
 };
 
-// Host threads for the loaders: all hardware threads, at most 64.
-int host_threads()
-{
-    const unsigned h = std::thread::hardware_concurrency();
-    return (int)std::max(1u, std::min(h, 64u));
-}
-
-// Run f(t, T) on T threads (t = 0..T-1); T = 1 runs inline.
-template <class F> void parallel(int T, F f)
-{
-    if (T <= 1) {
-        f(0, 1);
-        return;
-    }
-    std::vector<std::thread> th;
-    th.reserve((size_t)T);
-    for (int t = 0; t < T; t++) th.emplace_back(f, t, T);
-    for (auto &x : th) x.join();
-}
+using sbx::host_threads;
+using sbx::parallel;
 
 // construct_csr with every row kept: counting sort by row, then (col, value)
 // within the row, which is the order of std::sort on the tuples
