@@ -506,14 +506,17 @@ __device__ __forceinline__ void sb_update(double (&x)[V], double (&y)[V], const 
 // segment of LR*V agents); lane l of a row owns V consecutive agents (one
 // vector load of x and of y).  Per neighbour j the lane reads the sign word
 // of its agents in row j of the plane (lanes of one word share the address)
-// and counts into byte counters (count_unit); the new signs of the V agents
-// are OR-combined across the lanes of a word and written once.
+// and counts into byte counters (count_unit, CM = 0) or bit planes
+// (count_bits, CM = 1); the new signs of the V agents are OR-combined across
+// the lanes of a word and written once.
 //
 // Heavy rows (BIG kernels: +-1 weights, degree > kHeavy) come first, as
 // items of kHeavy neighbours: each leaves its byte counters in P.part, and
 // the warp completing a row's last chunk (a per-row counter, re-armed by that
 // warp) sums them and updates the row.  The other rows follow, in decreasing
-// degree when P.order is set.
+// degree when P.order is set; in a BIG byte-counter kernel those of
+// P.bits_min or more neighbours are counted in bit planes (mixed mode).
+// Isolated rows (the last P.niso entries of the order) are left to k_iso.
 // Resident CTAs per SM asked of the register allocator (measured on GB300):
 // 6 for heavy-row kernels, 4 for bit-plane counting (its loads in flight
 // need registers), 5 otherwise.
