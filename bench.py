@@ -265,6 +265,10 @@ def main():
                          "count mode 1 bytes / 2 bit planes); default: the fixed heuristic")
     ap.add_argument("--legs", default="all", choices=["all", "main"],
                     help="main: only the timed solves of the main precision (profiling)")
+    ap.add_argument("--instances", type=int, default=0, metavar="K",
+                    help="--profile, batch512: only the first K instances (sub-batch sizes)")
+    ap.add_argument("--step-times", action="store_true",
+                    help="--profile: time every step kernel (events) and print microseconds per step")
     args = ap.parse_args()
     wl = dict(WORKLOADS[args.workload])
     if args.sb_steps:
@@ -489,13 +493,17 @@ def run_profile_case(args, wl):
             "split": sbx.KERNEL_RESIDENT_SPLIT}[args.kernel]
     kw = dict(dt=wl["dt"], steps=wl["sb_steps"], run_steps=args.profile, seed=INIT_SEED,
               precision=sbx.PRECISIONS[wl["precision"]], kernel=kern,
-              flags=sbx.FLAG_NO_GRAPH | sbx.FLAG_NO_TUNE)
+              flags=sbx.FLAG_NO_GRAPH | sbx.FLAG_NO_TUNE | (sbx.FLAG_PROFILE if args.step_times else 0))
     if args.tile:
         v, lr, bt, cm = (int(t) for t in args.tile.split(","))
         kw.update(lane_agents=v, row_lanes=lr, block_threads=bt, count_mode=cm)
     ctx = sbx.Context(0)
+    size = {}
     if wl["kind"] == "batch":
         graphs = batch_instances(wl)
+        if args.instances:
+            graphs = graphs[:args.instances]
+        size = {"instances": len(graphs), "rows": sum(g.n for g in graphs), "nnz": sum(g.nnz for g in graphs)}
         probs = [ctx.problem(g) for g in graphs]
         res, _, t = ctx.solve_batch(probs, [wl["agents"]] * len(probs), sbx.params(fused=wl["fused"], **kw))
         r = res[0]
@@ -507,9 +515,12 @@ def run_profile_case(args, wl):
         else:
             prob = ctx.tsp_problem(inst["packed"], inst["N"], A=inst["A"], B=inst["B"], C_=inst["C"])
         r, _ = ctx.solve(prob, sbx.params(agents=wl["agents"], **kw))
-    print(json.dumps({"profile": wl["workload"], "steps_run": r["steps_run"], "kernel": r["kernel_used"],
-                      "tile": [r["lane_agents"], r["row_lanes"], r["block_threads"], r["count_mode"]],
-                      "time_us": r["time_us"]}), flush=True)
+    line = {"profile": wl["workload"], "steps_run": r["steps_run"], "kernel": r["kernel_used"],
+            "tile": [r["lane_agents"], r["row_lanes"], r["block_threads"], r["count_mode"]],
+            "time_us": r["time_us"], **size}
+    if args.step_times and r["steps_run"]:
+        line["step_us"] = 1000.0 * r["kernel_ms"] / r["steps_run"]
+    print(json.dumps(line), flush=True)
     ctx.close()
 
 
