@@ -62,7 +62,7 @@ PBYTES = {"f32": 4, "bf16": 2, "f16": 2, "f64": 8}
 TRAFFIC = {
     "torus": (45.85e6, "profiles/k_resident_rs_bf16_torus100x100.md (20,000-step launch)"),
     # per SB step: the k_row launch plus 1/100 of the isolated rows' k_iso
-    "rmat20": (9.886e8, "profiles/k_row_bf16_rmat20.md (k_row launch + k_iso/100)"),
+    "rmat20": (9.814e8, "profiles/k_row_bf16_rmat20.md (k_row launch + k_iso/100)"),
     "batch512": (1.3268e9, "profiles/k_row_bf16_batch512.md"),
 }
 
