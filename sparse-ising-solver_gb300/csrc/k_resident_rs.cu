@@ -60,12 +60,21 @@ __device__ __forceinline__ uint32_t row_step(const RsP &P, int s, uint4 &xv, uin
     if (P.unit) {
         // byte counters of 2 * count (deg <= 127), as the streaming kernel
         uint32_t lo = 0, hi = 0;
-#pragma unroll 4
-        for (int32_t e = e0; e < e1; e++) {
-            const uint32_t cw = __ldg(&P.colw[e]);
+        auto add = [&](uint32_t cw) {
             const uint32_t b = (uint32_t)Sin[cw & 0x7fffffffu] ^ (0u - (cw >> 31));
             lo += spread2x(b & 0xfu);
             hi += spread2x((b >> 4) & 0xfu);
+        };
+        if (deg == 4 && (e0 & 3) == 0) {
+            // four neighbours on a 16-byte boundary (lattices): one vector load
+            const uint4 c4 = __ldg((const uint4 *)(P.colw + e0));
+            add(c4.x);
+            add(c4.y);
+            add(c4.z);
+            add(c4.w);
+        } else {
+#pragma unroll 4
+            for (int32_t e = e0; e < e1; e++) add(__ldg(&P.colw[e]));
         }
         const float bias = 8388608.0f + (float)deg;
 #pragma unroll
