@@ -165,7 +165,8 @@ void free_csr(DevCsr &J)
 
 // Upload a validated CSR; classify its weights.
 int upload_csr(sbx_ctx *ctx, DevCsr &J, int64_t n, int64_t nnz, const int32_t *rowptr,
-               const int32_t *col, const double *val, double wsum, bool weights_always = false)
+               const int32_t *col, const double *val, double wsum, bool weights_always = false,
+               bool keep_host = true)
 {
     if (n <= 0 || n > INT32_MAX - 1 || nnz < 0 || nnz > INT32_MAX || !rowptr || (nnz && (!col || !val)))
         return fail(ctx, SBX_ERR_ARG, "bad CSR sizes or pointers");
@@ -263,9 +264,11 @@ int upload_csr(sbx_ctx *ctx, DevCsr &J, int64_t n, int64_t nnz, const int32_t *r
     J.max_deg = maxdeg;
     J.skewed = (double)maxdeg > 8.0 * std::max(1.0, (double)nnz / (double)n);
     J.niso = niso;
-    J.hval.assign(val, val + nnz);
-    J.hrowptr.assign(rowptr, rowptr + n + 1);
-    J.hcol.assign(col, col + nnz);
+    if (keep_host) {   // else the caller moves its arrays in
+        J.hval.assign(val, val + nnz);
+        J.hrowptr.assign(rowptr, rowptr + n + 1);
+        J.hcol.assign(col, col + nnz);
+    }
     J.hperm = perm;
     CK(cudaMalloc(&J.rowptr, sizeof(int32_t) * (n + 1)));
     CK(cudaMalloc(&J.colw, sizeof(uint32_t) * std::max<int64_t>(nnz, 1)));
@@ -994,34 +997,45 @@ int solve_tsp(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
 // Pack the instances of one agent class into a block-diagonal matrix.
 int build_class(sbx_ctx *ctx, BatchClass &c)
 {
+    const size_t ni = c.probs.size();
     int64_t n = 0, nnz = 0;
-    for (const sbx_problem *p : c.probs) {
+    std::vector<int64_t> e_off(ni + 1, 0);
+    for (size_t i = 0; i < ni; i++) {
+        const sbx_problem *p = c.probs[i];
         c.row_off.push_back(n);
         n += p->J.n;
         nnz += p->J.nnz;
-        c.xi0.push_back(xi0_of(p->J));
+        e_off[i + 1] = nnz;
         c.wsum.push_back(p->J.wsum);
     }
     if (n > INT32_MAX - 1 || nnz > INT32_MAX) return fail(ctx, SBX_ERR_UNSUPPORTED, "batch too large for int32 indices");
     std::vector<int32_t> rp((size_t)n + 1), col((size_t)nnz), rinst((size_t)n);
     std::vector<double> val((size_t)nnz);
-    int64_t e = 0;
-    for (size_t i = 0; i < c.probs.size(); i++) {
-        const DevCsr &J = c.probs[i]->J;
-        const int64_t r0 = c.row_off[i];
-        for (int64_t r = 0; r < J.n; r++) {
-            rp[r0 + r] = (int32_t)(e + J.hrowptr[r]);
-            rinst[r0 + r] = (int32_t)i;
+    c.xi0.assign(ni, 0.0);
+    // instances on host threads: each one's xi0 (its sums in the reference's
+    // order) and its block of the block-diagonal matrix
+    const int T = nnz > (1 << 20) ? host_threads() : 1;
+    parallel(T, [&](int t, int TT) {
+        for (size_t i = (size_t)t; i < ni; i += (size_t)TT) {
+            const DevCsr &J = c.probs[i]->J;
+            c.xi0[i] = xi0_of(J);
+            const int64_t r0 = c.row_off[i], e = e_off[i];
+            for (int64_t r = 0; r < J.n; r++) {
+                rp[r0 + r] = (int32_t)(e + J.hrowptr[r]);
+                rinst[r0 + r] = (int32_t)i;
+            }
+            for (int64_t k = 0; k < J.nnz; k++) {
+                col[e + k] = (int32_t)(J.hcol[k] + r0);
+                val[e + k] = J.hval[k];
+            }
         }
-        for (int64_t k = 0; k < J.nnz; k++) {
-            col[e + k] = (int32_t)(J.hcol[k] + r0);
-            val[e + k] = J.hval[k];
-        }
-        e += J.nnz;
-    }
+    });
     rp[n] = (int32_t)nnz;
-    int rc = upload_csr(ctx, c.J, n, nnz, rp.data(), col.data(), val.data(), 0.0);
+    int rc = upload_csr(ctx, c.J, n, nnz, rp.data(), col.data(), val.data(), 0.0, false, false);
     if (rc) return rc;
+    c.J.hrowptr = std::move(rp);
+    c.J.hcol = std::move(col);
+    c.J.hval = std::move(val);
     CK(cudaMalloc(&c.J.rinst, sizeof(int32_t) * n));
     CK(cudaMalloc(&c.J.c0r32, sizeof(float) * n));
     CK(cudaMalloc(&c.J.c0r64, sizeof(double) * n));
