@@ -482,13 +482,7 @@ bool poll_stop(sbx_ctx *ctx, int64_t c, bool force_all)
 // The state (x and y) is more than half of L2: it streams from DRAM each step.
 bool state_exceeds_half_l2(const SolveDims &d)
 {
-    static int l2 = -1;
-    if (l2 < 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess) l2 = 0;
-    }
-    return 2.0 * (double)d.n * d.Ap * prec_bytes(d.prec) > 0.5 * (double)l2;
+    return 2.0 * (double)d.n * d.Ap * prec_bytes(d.prec) > 0.5 * (double)dev_attr(cudaDevAttrL2CacheSize);
 }
 
 // A tile the step kernels are built for (k_step.cuh, step_kw): whole-warp

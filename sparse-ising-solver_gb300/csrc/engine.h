@@ -32,6 +32,15 @@ constexpr int kBitsMin = 12;
 
 inline size_t prec_bytes(int p) { return p == P_F64 ? 8 : p == P_F32 ? 4 : 2; }
 
+// An attribute of the calling thread's current device (0 when the query
+// fails); queried each time, so contexts on different devices see their own.
+inline int dev_attr(cudaDeviceAttr a)
+{
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&v, a, dev) != cudaSuccess) return 0;
+    return v;
+}
+
 // MaxCut / QUBO matrix on the device.  colw holds the column index; when every
 // weight is +-1 ("unit"), bit 31 holds the weight's sign and no value array is
 // read by the step kernels.

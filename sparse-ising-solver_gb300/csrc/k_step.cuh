@@ -850,12 +850,7 @@ template <class K>
 cudaError_t launch_grid(K kern, const SolveDims &d, int64_t items, int bt, size_t smem, cudaStream_t s,
                         const StepP &P, int offset)
 {
-    static int nsm = 0;
-    if (!nsm) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    }
+    const int nsm = std::max(1, dev_attr(cudaDevAttrMultiProcessorCount));
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, bt, smem);
     if (per_sm < 1) per_sm = 1;
@@ -1097,12 +1092,7 @@ cudaError_t iso_t(const SolveDims &d, const DevCsr &J, const StepP &P, cudaStrea
 {
     constexpr int V = 16 / (int)sizeof(T);
     if (!P.niso || !P.order || d.Ap % 32) return cudaErrorInvalidValue;
-    static int nsm = 0;
-    if (!nsm) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    }
+    const int nsm = std::max(1, dev_attr(cudaDevAttrMultiProcessorCount));
     const size_t smem = sizeof(uint32_t) * d.W;
     const int64_t warps = (P.niso * (d.Ap / V) + 31) / 32;
     const int64_t blocks = std::min<int64_t>((warps + 4 * 8 - 1) / (4 * 8), (int64_t)nsm * 64);

@@ -176,14 +176,8 @@ StepP make_step(const SolveDims &d, const DevCsr &J, Work &w)
     P.zrow = (uint32_t)d.n;
     P.W = d.W;
     {
-        static int l2 = -1;
-        if (l2 < 0) {
-            int dev = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
-        }
         const double state = 2.0 * (double)d.n * d.Ap * prec_bytes(d.prec);
-        P.stream_state = state > 0.5 * (double)l2 ? 1 : 0;
+        P.stream_state = state > 0.5 * (double)dev_attr(cudaDevAttrL2CacheSize) ? 1 : 0;
     }
     P.Ap = d.Ap;
     P.c0 = d.c0;
