@@ -1,20 +1,23 @@
 """Benchmark of the SB hot path: nnz*agent*steps/s on one GB300.
 
-Default workload (the metric's headline configuration): MaxCut on a 2-D torus
-100x100 (n = 10,000, degree 4, weights +-1 from seed 1234), 1024 agents,
-dt = 0.5, fused kernel, 20,000 steps, update window on (early exit once every
-agent has bifurcated).  A bench "step" is one complete solve of the instance
-(device init from the seed, the SB loop, windows, the cut reduction).
-`value` is the BF16-state run with the problem resident on the device; the
-FP32 run and the FP64 run (the energy-error reference) of the same seed are
-reported beside it.  `e2e` repeats the BF16 solve through the C ABI from host
-buffers: CSR upload, solve and per-agent cut read-back are inside the timed
-region.  Other workloads (--workload): er800 (ER n=800, FP32 plain, 10k
-steps), rmat20 (R-MAT 2^20, 256 agents, BF16), tsp30 (30 cities, FP32),
-batch512 (512 ER/RGG instances of 100..20000 vertices, 64 agents, BF16).
+Default workload (the configuration the metric names, "BF16-batched vs
+FP32-plain"): 512 independent MaxCut instances, n log-uniform in [100, 20000],
+Erdos-Renyi and random geometric graphs of average degree 6-40, weights +-1,
+64 agents each, BF16 state, dt 0.5, 10,000 steps, all instances in one
+launch per SB step (a CUDA graph per window).  A bench "step" is one complete
+batched solve (device init from the seeds, the SB loop, windows, the exact
+cuts).  `value` has the problems resident on the device; `e2e` goes through
+the C ABI from host buffers (every instance's CSR uploaded, the solve, the
+per-agent cuts read back).  FP32-plain (each instance solved alone in FP32),
+the FP64 run of the same seeds (the energy error) and the time to reach
+FP32-plain's best cuts are reported beside it.
+
+Other workloads (--workload): torus (torus 100x100, 1024 agents, BF16,
+update window), er800 (ER n=800, 1024 agents, FP32 plain), rmat20 (R-MAT
+2^20, 256 agents, BF16), tsp30 (30 cities, 1024 agents, FP32).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload torus|er800|rmat20|tsp30|batch512]
+                  [--workload batch512|torus|er800|rmat20|tsp30]
 """
 import argparse
 import json
@@ -47,7 +50,7 @@ WORKLOADS = {
     # unit scale its dynamics find no valid tour (checked with the oracle)
     "tsp30": dict(kind="tsp", workload="tsp-30-unit-square-x1000-penalty1.5maxd", cities=30,
                   coord_scale=1000.0, agents=1024, dt=0.1, sb_steps=20000, precision="f32",
-                  compare=("bf16",)),
+                  compare=("bf16", "f64")),
     "batch512": dict(kind="batch", workload="batch-512-maxcut-er+rgg-n100..20000-pm1",
                      instances=512, agents=64, dt=0.5, sb_steps=10000, fused=1,
                      precision="bf16", compare=("f32",)),
@@ -56,14 +59,18 @@ GRAPH_SEED, INIT_SEED = 1234, 1
 PBYTES = {"f32": 4, "bf16": 2, "f16": 2, "f64": 8}
 
 
-# DRAM traffic (read + write bytes) per launch of each workload's dominant
-# kernel, from the ncu captures summarised in profiles/ (the same kernel and
-# tile the bench runs; the resident kernels' launch covers the whole solve).
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of
+# each workload's dominant kernel, from one ncu capture of the same kernel
+# and tile (the command is in the source string); the resident kernels'
+# launch covers the whole solve.
 TRAFFIC = {
-    "torus": (45.85e6, "profiles/k_resident_rs_bf16_torus100x100.md (20,000-step launch)"),
+    "torus": (45.85e6, "ncu --set full -k regex:k_resident_rs -c 1: bench.py --workload torus "
+                       "--profile 20000 --kernel split (one 20,000-step launch)"),
     # per SB step: the k_row launch plus 1/100 of the isolated rows' k_iso
-    "rmat20": (9.814e8, "profiles/k_row_bf16_rmat20.md (k_row launch + k_iso/100)"),
-    "batch512": (1.3268e9, "profiles/k_row_bf16_batch512.md"),
+    "rmat20": (9.814e8, "ncu --set full -k regex:k_row|k_iso: bench.py --workload rmat20 "
+                        "--profile 100 (k_row launch + k_iso / 100)"),
+    "batch512": (1.3268e9, "ncu --set full -k regex:k_row -s 4 -c 1: bench.py --workload batch512 "
+                           "--profile 100 --tile 8,8,128,2"),
 }
 
 
@@ -126,36 +133,55 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def batch_instances(wl):
-    """512 (by default) seeded MaxCut instances: n log-uniform in [100, 20000],
-    even ones Erdos-Renyi with average degree uniform in [6, 40], odd ones
-    random geometric graphs of the same degree range; weights +-1."""
+def batch_specs(count):
+    """The batched workload's instances as (kind, n, degree, seed): n
+    log-uniform in [100, 20000], even positions Erdos-Renyi with average
+    degree uniform in [6, 40], odd ones random geometric graphs of the same
+    degree range; weights +-1."""
     import numpy as np
-    import sbx
     rng = np.random.default_rng(GRAPH_SEED)
     out = []
-    for i in range(wl["instances"]):
+    for i in range(count):
         n = int(round(np.exp(rng.uniform(np.log(100), np.log(20000)))))
         deg = float(rng.uniform(6, 40))
-        if i % 2 == 0:
-            out.append(sbx.gen_er(n, min(1.0, deg / (n - 1)), pm1=True, seed=GRAPH_SEED + i))
-        else:
-            out.append(sbx.gen_rgg(n, deg, seed=GRAPH_SEED + i))
+        out.append(("er" if i % 2 == 0 else "rgg", n, deg, GRAPH_SEED + i))
     return out
 
 
-def build_instance(wl):
-    """The seeded synthetic instance: a Graph, or a dict with the TSP data."""
-    import sbx
+def batch_graph(spec, gen):
+    """One batched instance from its spec, built by `gen`: the engine's
+    generators (sbx) or their restatement on the oracle side (sbo), which
+    give the same arrays."""
+    kind, n, deg, seed = spec
+    if kind == "er":
+        return gen.gen_er(n, min(1.0, deg / (n - 1)), pm1=True, seed=seed)
+    return gen.gen_rgg(n, deg, seed=seed)
+
+
+def batch_instances(wl, gen=None, count=0):
+    """The batch's graphs (the first `count` when given)."""
+    if gen is None:
+        import sbx as gen
+    specs = batch_specs(wl["instances"])
+    if count:
+        specs = specs[:count]
+    return [batch_graph(sp, gen) for sp in specs]
+
+
+def build_instance(wl, gen=None):
+    """The seeded synthetic instance: a Graph, or a dict with the TSP data,
+    built by `gen` (sbx by default; sbo on the CPU legs)."""
+    if gen is None:
+        import sbx as gen
     if wl["kind"] == "maxcut":
         g = wl["graph"]
         if g[0] == "torus":
-            return sbx.gen_torus(g[1], g[2], seed=GRAPH_SEED)
+            return gen.gen_torus(g[1], g[2], seed=GRAPH_SEED)
         if g[0] == "er":
-            return sbx.gen_er(g[1], g[2], pm1=g[3], seed=GRAPH_SEED)
-        return sbx.gen_rmat(g[1], g[2], seed=GRAPH_SEED)
-    xc, yc = sbx.gen_cities(wl["cities"], wl.get("coord_scale", 1.0), seed=GRAPH_SEED)
-    packed = sbx.tsp_distances(xc, yc, sbx.DIST_EUC_2D_FLOAT)
+            return gen.gen_er(g[1], g[2], pm1=g[3], seed=GRAPH_SEED)
+        return gen.gen_rmat(g[1], g[2], seed=GRAPH_SEED)
+    xc, yc = gen.gen_cities(wl["cities"], wl.get("coord_scale", 1.0), seed=GRAPH_SEED)
+    packed = gen.tsp_distances(xc, yc, 2)   # EUC_2D_FLOAT: no truncation
     mx = float(packed.max())
     return dict(xc=xc, yc=yc, packed=packed, N=wl["cities"], A=1.0, B=1.5 * mx, C=1.5 * mx)
 
@@ -174,10 +200,12 @@ def instance_sizes(wl, inst):
 
 
 def config_of(wl):
+    """The workload's configuration, printed identically by both arms."""
     c = {k: v for k, v in wl.items() if k not in ("compare", "graph")}
     if "graph" in wl:
         c["graph"] = list(wl["graph"])
     c["graph_seed"], c["init_seed"] = GRAPH_SEED, INIT_SEED
+    c["l2"] = "flushed between timed iterations (256 MB write)"
     return c
 
 
@@ -215,6 +243,40 @@ def cpu_sample(wl, inst, seconds=12.0, nthreads=0):
     return nnz * A * steps / dt, cores, s, dt
 
 
+def cpu_batch_sample(wl, graphs, seconds=10.0, cores=0):
+    """The FP64 oracle's fused step (the restatement of the reference kernel)
+    on every instance of the batch, s steps each, instances spread over the
+    host threads (one thread per instance at a time).  The initial state is
+    made before the timed region.  Returns (nnz*agent*steps/s, cores, s,
+    seconds)."""
+    import sbo
+    from concurrent.futures import ThreadPoolExecutor
+    cores = cores or (os.cpu_count() or 1)
+    A, dt, steps = wl["agents"], wl["dt"], wl["sb_steps"]
+    st = []
+    for i, g in enumerate(graphs):
+        og = sbo.Graph(g.n, g.rowptr, g.col, g.val, g.wsum)
+        x, y = sbo.init_maxcut(g.n, A, INIT_SEED + i)
+        sbo.update_xy(x, y, 0, steps, dt)
+        st.append([og, x, y, sbo.xi0(og), 0])
+    order = sorted(range(len(st)), key=lambda i: -st[i][0].nnz)
+
+    def run(k):
+        def work(i):
+            og, x, y, x0, k0 = st[i]
+            for j in range(k):
+                sbo.fused_step(og, x, y, A, k0 + j, steps, dt, x0, nthreads=1)
+            st[i][4] = k0 + k
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(cores) as ex:
+            list(ex.map(work, order))
+        return time.perf_counter() - t0
+    t1 = run(1)
+    s = int(max(1, min(wl["sb_steps"] // 2, seconds / max(t1, 1e-6))))
+    sec = run(s)
+    return sum(g.nnz for g in graphs) * A * s / sec, cores, s, sec
+
+
 def run_reference(args, wl, rank):
     """--impl reference: the reference path has no CPU solver, so its CPU
     implementation here is the FP64 oracle port, every host thread."""
@@ -222,13 +284,26 @@ def run_reference(args, wl, rank):
         return
     import sbo
     sbo.lib()
-    inst = build_instance(wl)
     vals, samples, cores = [], [], 1
-    for i in range(args.warmup + args.steps):
-        v, cores, s, dt = cpu_sample(wl, inst, seconds=8.0)
-        if i >= args.warmup:
-            vals.append(v)
-            samples.append((s, dt))
+    if wl["kind"] == "batch":
+        # the instances through the oracle's generators: nothing of the
+        # engine is loaded by this arm
+        graphs = batch_instances(wl, gen=sbo, count=args.instances)
+        for i in range(args.warmup + args.steps):
+            v, cores, s, dt = cpu_batch_sample(wl, graphs, seconds=4.0)
+            if i >= args.warmup:
+                vals.append(v)
+                samples.append((s, dt))
+        what = "FP64 oracle fused step, %d SB steps of each of the %d instances per bench step" % (
+            samples[0][0], len(graphs))
+    else:
+        inst = build_instance(wl, gen=sbo)
+        for i in range(args.warmup + args.steps):
+            v, cores, s, dt = cpu_sample(wl, inst, seconds=8.0)
+            if i >= args.warmup:
+                vals.append(v)
+                samples.append((s, dt))
+        what = "%d SB steps of the workload per bench step" % samples[0][0]
     value = sum(vals) / len(vals)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "nnz*agent*steps/s",
@@ -237,11 +312,14 @@ def run_reference(args, wl, rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded generators)", "config": config_of(wl),
         "cpu_baseline": {"value": value, "unit": "nnz*agent*steps/s", "cores": cores,
-                         "kind": "port",
-                         "sample": "%d SB steps of the workload per bench step" % samples[0][0]},
+                         "kind": "port", "sample": what},
         "e2e": {"value": value, "unit": "nnz*agent*steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
+    # the CPU arm runs the reference's path as the oracle restates it, and
+    # nothing of the engine
+    if "sbx" in sys.modules:
+        raise RuntimeError("the reference arm loaded the engine")
     print(json.dumps(line), flush=True)
 
 
@@ -251,7 +329,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="torus", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="batch512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--sb-steps", type=int, default=0,
                     help="SB steps per solve (profiling cases use fewer)")
@@ -266,7 +344,7 @@ def main():
     ap.add_argument("--legs", default="all", choices=["all", "main"],
                     help="main: only the timed solves of the main precision (profiling)")
     ap.add_argument("--instances", type=int, default=0, metavar="K",
-                    help="--profile, batch512: only the first K instances (sub-batch sizes)")
+                    help="batch512: only the first K instances (sub-batch sizes)")
     ap.add_argument("--step-times", action="store_true",
                     help="--profile: time every step kernel (events) and print microseconds per step")
     args = ap.parse_args()
@@ -462,9 +540,9 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_main,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": main_prec, "data": "synthetic (seeded generators)",
-            "config": dict(config_of(wl), state="%s storage, fp32 arithmetic, exact integer force"
-                           % main_prec, l2="flushed between iterations (256 MB write)",
-                           parallelism="replicas" if world > 1 else "single", n=n, nnz=nnz),
+            "config": config_of(wl),
+            "shape": {"n": n, "nnz": nnz, "parallelism": "replicas" if world > 1 else "single",
+                      "state": "%s storage, fp32 arithmetic, exact integer force" % main_prec},
             "e2e": {"value": e2e, "unit": "nnz*agent*steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
@@ -500,9 +578,7 @@ def run_profile_case(args, wl):
     ctx = sbx.Context(0)
     size = {}
     if wl["kind"] == "batch":
-        graphs = batch_instances(wl)
-        if args.instances:
-            graphs = graphs[:args.instances]
+        graphs = batch_instances(wl, count=args.instances)
         size = {"instances": len(graphs), "rows": sum(g.n for g in graphs), "nnz": sum(g.nnz for g in graphs)}
         probs = [ctx.problem(g) for g in graphs]
         res, _, t = ctx.solve_batch(probs, [wl["agents"]] * len(probs), sbx.params(fused=wl["fused"], **kw))
@@ -527,7 +603,8 @@ def run_profile_case(args, wl):
 def run_batch(args, wl, rank, world, local):
     """The batched workload: every instance packed into one block-diagonal
     run per bench step (sbx_solve_batch), against the FP32-plain mode (each
-    instance solved alone, FP32 state) for throughput and best cut."""
+    instance solved alone, FP32 state) for throughput, best cut and time to
+    target, and against the FP64 run of the same seeds for the energy error."""
     import numpy as np
     import torch
     import sbx
@@ -540,11 +617,13 @@ def run_batch(args, wl, rank, world, local):
     torch.cuda.set_stream(stream)
     ctx = sbx.Context(local)
     ctx.set_stream(stream.cuda_stream)
-    graphs = batch_instances(wl)
+    graphs = batch_instances(wl, count=args.instances)
     A = wl["agents"]
     agents = [A] * len(graphs)
     probs = [ctx.problem(g) for g in graphs]
-    units_per = sum(g.nnz for g in graphs) * A
+    n_tot = sum(g.n for g in graphs)
+    nnz_tot = sum(g.nnz for g in graphs)
+    units_per = nnz_tot * A
     seed = INIT_SEED + rank
     prm = lambda prec, flags=0: sbx.params(dt=wl["dt"], steps=wl["sb_steps"], seed=seed,
                                            fused=wl["fused"], precision=sbx.PRECISIONS[prec],
@@ -552,11 +631,13 @@ def run_batch(args, wl, rank, world, local):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     for _ in range(args.warmup):
         ctx.solve_batch(probs, agents, prm(wl["precision"]))
+    if world > 1:
+        dist.barrier()
     torch.cuda.synchronize()
     evs, res = [], None
     with Clocks(local) as clk:
         for _ in range(args.steps):
-            flush.fill_(1)
+            flush.fill_(1)   # L2 flush between iterations
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
@@ -571,14 +652,23 @@ def run_batch(args, wl, rank, world, local):
     value = units_all / (ms / 1000.0)
     best_b = np.array([r["max"] for r in res])
     launches = res[0]["gpu_launches"]
-    # e2e: upload every instance from host buffers, solve, read back
-    t0 = time.perf_counter()
-    p2 = [ctx.problem(g) for g in graphs]
-    ctx.solve_batch(p2, agents, prm(wl["precision"]))
-    for p in p2:
-        p.close()
-    torch.cuda.synchronize()
-    e2e = units_per * steps_run / (time.perf_counter() - t0)
+
+    # e2e through the C ABI from host buffers: every instance's CSR uploaded
+    # (sbx_problem_csr), the batched solve, the per-agent cuts read back
+    e2e_w, e2e_k = min(args.warmup, 2), max(1, min(args.steps, 5))
+    t_e2e = []
+    for i in range(e2e_w + e2e_k):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p2 = [ctx.problem(g) for g in graphs]
+        ctx.solve_batch(p2, agents, prm(wl["precision"]))
+        for p in p2:
+            p.close()
+        torch.cuda.synchronize()
+        if i >= e2e_w:
+            t_e2e.append(time.perf_counter() - t0)
+    e2e = units_per * steps_run / (sum(t_e2e) / len(t_e2e))
+
     # FP32-plain: each instance alone (seed + i, as the batch seeds it)
     t_plain, best_p = 0.0, []
     for i, p in enumerate(probs):
@@ -589,6 +679,11 @@ def run_batch(args, wl, rank, world, local):
     best_p = np.array(best_p)
     v_plain = units_per * wl["sb_steps"] / t_plain
     rel = (best_p - best_b) / np.abs(best_p)
+    # the FP64 run of the same seeds (bit-exact with the FP64 oracle): the
+    # energy error of the batch's best cuts
+    r64, _, _ = ctx.solve_batch(probs, agents, prm("f64"))
+    best_64 = np.array([r["max"] for r in r64])
+    err64 = np.abs(best_b - best_64) / np.abs(best_64)
     # Time to target: per instance, the FP32-plain best cut less 0.1%.  The
     # batch reaches all targets when its slowest instance does; FP32-plain
     # solves the instances one after another.
@@ -607,43 +702,54 @@ def run_batch(args, wl, rank, world, local):
            "batched_all_us": float(tb.max()) if reached.all() else None,
            "batched_reached_us": float(tb[reached].max()) if reached.any() else None,
            "fp32_plain_us": float(tp.sum()),
-           "speedup": float(tp.sum() / tb.max()) if reached.all() else None}
+           "speedup": float(tp.sum() / tb.max()) if reached.all() else None,
+           "missed": [int(i) for i in np.nonzero(~reached)[0]]}
     peaks, peak_kind = load_peaks()
-    n_tot = sum(g.n for g in graphs)
-    nnz_tot = sum(g.nnz for g in graphs)
-    b_step = 2 * n_tot * A * 4 + 8 * nnz_tot + 4 * (n_tot + len(graphs))
+    b_step = 2 * n_tot * A * (PBYTES[wl["precision"]] * 2) + 8 * nnz_tot + 4 * (n_tot + len(graphs))
     rp, _, _ = ctx.solve_batch(probs, agents, prm(wl["precision"], sbx.FLAG_PROFILE))
     roof = None
     if rp[0]["kernel_ms"] > 0:
         per_launch_s = rp[0]["kernel_ms"] / 1000.0 / rp[0]["steps_run"]
         achieved = b_step / per_launch_s / 1e9
-        tr = TRAFFIC["batch512"]
+        tr = TRAFFIC.get("batch512") if not args.instances else None
         roof = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": tr[0], "traffic_source": tr[1],
-                "peak_kind": peak_kind, "kernel": "k_row per SB step over all instances",
-                "bytes_per_launch": b_step, "launch_us": per_launch_s * 1e6}
+                "frac": achieved / peaks["hbm_gbs"], "traffic": tr[0] if tr else None,
+                "traffic_source": tr[1] if tr else None, "peak_kind": peak_kind,
+                "kernel": "step kernel, one launch per SB step over all instances",
+                "bytes_per_launch": b_step, "launch_us": per_launch_s * 1e6,
+                "launches": rp[0]["kernel_launches"]}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, cores, s_cpu, dt = cpu_batch_sample(wl, graphs, seconds=10.0)
+        cpu = {"value": v, "unit": "nnz*agent*steps/s", "cores": cores, "kind": "port",
+               "sample": "FP64 oracle fused step, %d SB steps of each of the %d instances "
+                         "(%.1f s)" % (s_cpu, len(graphs), dt)}
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "nnz*agent*steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": wl["precision"], "data": "synthetic (seeded generators)",
-            "config": dict(config_of(wl), rows=n_tot, nnz=nnz_tot,
-                           l2="flushed between iterations (256 MB write)"),
+            "config": config_of(wl),
+            "shape": {"instances": len(graphs), "rows": n_tot, "nnz": nnz_tot,
+                      "parallelism": "replicas" if world > 1 else "single"},
             "e2e": {"value": e2e, "unit": "nnz*agent*steps/s",
                     "h2d_bytes_per_step": int(sum(g.rowptr.nbytes + g.col.nbytes + g.val.nbytes
                                                   for g in graphs)),
-                    "d2h_bytes_per_step": int(8 * A * len(graphs))},
-            "gpu_launches": launches, "roofline": roof, "cpu_baseline": None,
+                    "d2h_bytes_per_step": int(8 * A * len(graphs)),
+                    "warmup": e2e_w, "samples": e2e_k},
+            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "fp32_plain": {"value": v_plain, "speedup_of_batched": value / v_plain,
                            "seconds": t_plain},
             "quality": {"instances": len(graphs),
                         "within_0.1pct_of_fp32_plain": float(np.mean(rel <= 1e-3)),
-                        "mean_rel_gap": float(np.mean(rel)), "max_rel_gap": float(np.max(rel))},
+                        "mean_rel_gap": float(np.mean(rel)), "max_rel_gap": float(np.max(rel)),
+                        "energy_error_vs_f64": {"mean": float(np.mean(err64)),
+                                                "max": float(np.max(err64))}},
             "time_to_target": ttt,
-            "tile": {k: res[0][k] for k in ("lane_agents", "row_lanes", "block_threads", "count_mode",
-                                            "staging")},
+            "tile": {k: res[0][k] for k in ("kernel_used", "lane_agents", "row_lanes",
+                                            "block_threads", "count_mode", "staging")},
         }
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -53,6 +53,12 @@ enum { SBX_DIST_EUC_2D = 0, SBX_DIST_GEO = 1, SBX_DIST_EUC_2D_FLOAT = 2 };
 #define SBX_FLAG_NO_GRAPH 2u    /* launch kernels directly, not through a graph */
 #define SBX_FLAG_PROFILE 4u     /* time every hot-kernel launch with events */
 #define SBX_FLAG_NO_TUNE 8u     /* streaming tile from the fixed heuristic, not timed */
+/* Test only: every bounded device wait of the solve (the co-resident window
+ * barrier, the staged-row copy waits) gives up at its first check, as a wait
+ * that never completes would after its limit.  The kernels flag the error,
+ * let their copies in flight land and return; the solve returns SBX_ERR_CUDA
+ * and the context stays usable for the next solve. */
+#define SBX_FLAG_TEST_GIVEUP 16u
 
 typedef struct sbx_ctx sbx_ctx;
 typedef struct sbx_problem sbx_problem;
@@ -175,6 +181,15 @@ int sbx_solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems,
                     const double *targets, sbx_result *res, double *agent_values,
                     double *batch_time_us);
 
+/* State of instance `index` (its position in the last sbx_solve_batch
+ * call), as sbx_get_state: x, y, spins [n_i * agents_i] each, row-major.
+ * No counterpart in the reference (it has no batched solve).  Instances are
+ * solved one agent class (padded agent count) after another in the same
+ * buffers, so only the last class's instances are available; others give
+ * SBX_ERR_STATE, as does any call after a later sbx_solve. */
+int sbx_get_batch_state(sbx_ctx *ctx, int32_t index, double *x, double *y,
+                        int32_t *spins);
+
 /* ---- fused steps without device allocation ---- */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory (a process whose device memory is all held by its own arena, or a
@@ -186,10 +201,12 @@ int sbx_solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems,
  * only scratch, two sign planes, lives in a static device array of
  * 2 * SBX_NOALLOC_MAX_WORDS words (16 MiB, held by every GPU that loads the
  * library); n * agents / 32 must not exceed SBX_NOALLOC_MAX_WORDS and agents
- * must be a multiple of 32, else SBX_ERR_ARG.  The first call on a device
- * looks up the array's device address (make it before any stream capture);
- * calls share the array, so calls that overlap on the GPU race.  Nothing is
- * allocated or freed. */
+ * must be a multiple of 32, else SBX_ERR_ARG.  Every pointer must be valid,
+ * d_col and d_val too when the matrix has no entries (NULL: SBX_ERR_ARG).
+ * The first call on a device looks up the array's device address (make it
+ * before any stream capture) and keeps it for the process: after a device
+ * reset the entry point must not be called again.  Calls share the array,
+ * so calls that overlap on the GPU race.  Nothing is allocated or freed. */
 #define SBX_NOALLOC_MAX_WORDS (1 << 21)
 int sbx_fused_steps_noalloc(const int32_t *d_rowptr, const int32_t *d_col,
                             const float *d_val, int64_t n, int32_t agents,

@@ -21,6 +21,8 @@
  *   - src/ising_tsp.cu:50-287  TSP orchestration    -> sbo_tsp_solve
  *   - src/csr.cpp:15-192       MTX loader, CSR      -> sbo_mtx_load, sbo_dense_to_csr
  *   - src/tsp_cpu.cpp:9-45     TSPLIB loader        -> sbo_tsplib_load
+ * and, in sbo_lp.c, the same MaxCut path in the engine's FP32 / BF16 / FP16
+ * state modes (float arithmetic, rounded to the storage type on each store).
  *
  * Floating-point semantics: every operation is a separately rounded IEEE
  * double operation in the order the reference source writes it (the library
@@ -74,6 +76,9 @@ typedef struct {
     uint32_t seed;         /* srand() seed */
     int32_t schedule;      /* SBO_JACOBI or SBO_SERIAL */
     int32_t nthreads;      /* OpenMP threads for SBO_JACOBI (<=0: all) */
+    int32_t run_steps;     /* run only the windows covering the first
+                              run_steps steps of the `steps` schedule
+                              (0: all of them) */
 } sbo_params;
 
 typedef struct {
@@ -108,6 +113,20 @@ void sbo_stats(const double *v, int64_t A, sbo_result *r);
 int sbo_maxcut_solve(const sbo_csr *J, const sbo_params *p, sbo_result *r,
                      double *cut, double *x, double *y, int32_t *spins);
 
+/* ---- MaxCut in the engine's lower-precision state modes (sbo_lp.c) ---- */
+/* Storage precisions (the engine's SBX_F32, SBX_BF16, SBX_F16 values). */
+enum { SBO_F32 = 0, SBO_BF16 = 1, SBO_F16 = 2 };
+float sbo_round_storage(int prec, float v);
+void sbo_init_maxcut_lp(int64_t n, int64_t A, uint32_t seed, int prec, float *x,
+                        float *y);
+void sbo_update_xy_lp(float *x, float *y, int64_t count, int32_t step,
+                      int32_t max_steps, double dt, int prec);
+/* As sbo_maxcut_solve, with float state rounded to `prec` on every store;
+ * x, y (n*A floats) and spins may be NULL. */
+int sbo_maxcut_solve_lp(const sbo_csr *J, const sbo_params *p, int prec,
+                        sbo_result *r, double *cut, float *x, float *y,
+                        int32_t *spins);
+
 /* ---- TSP ---- */
 int sbo_tsp_distances(int32_t N, const double *xc, const double *yc, int kind,
                       double *packed);
@@ -130,6 +149,23 @@ int sbo_tsp_solve(const sbo_csr *J, int32_t N, const double *packed,
                   const double *rowsum, double qa, double qb, double qc,
                   const sbo_params *p, sbo_result *r, double *lengths,
                   int32_t *tours, double *x, double *y, int32_t *valid_list);
+
+/* ---- seeded synthetic instances (sbo_gen.c) ---- */
+/* A generated graph: arrays malloc'ed by the generator, freed by
+ * sbo_graph_free. */
+typedef struct {
+    int64_t n, nnz;
+    int32_t *rowptr, *col;
+    double *val;
+    double wsum;
+} sbo_graph;
+void sbo_graph_free(sbo_graph *g);
+int sbo_gen_er(int64_t n, double p, int pm1, uint64_t seed, sbo_graph *out);
+int sbo_gen_torus(int32_t rows, int32_t cols, uint64_t seed, sbo_graph *out);
+int sbo_gen_rmat(int32_t scale, int32_t edge_factor, double a, double b, double c,
+                 uint64_t seed, sbo_graph *out);
+int sbo_gen_rgg(int64_t n, double avg_degree, uint64_t seed, sbo_graph *out);
+int sbo_gen_cities(int32_t N, double scale, uint64_t seed, double *xc, double *yc);
 
 /* ---- loaders ---- */
 /* csr.cpp:15-109 + construct_csr (:157-192) with empty rows kept.

@@ -30,7 +30,7 @@ class Params(C.Structure):
     _fields_ = [("dt", C.c_double), ("steps", C.c_int32), ("agents", C.c_int32),
                 ("fused", C.c_int32), ("uw", C.c_int32), ("period", C.c_int32),
                 ("threshold", C.c_int32), ("seed", C.c_uint32),
-                ("schedule", C.c_int32), ("nthreads", C.c_int32)]
+                ("schedule", C.c_int32), ("nthreads", C.c_int32), ("run_steps", C.c_int32)]
 
 
 class Result(C.Structure):
@@ -81,10 +81,75 @@ class Graph:
                    self.val.ctypes.data, self.wsum)
 
 
+class _GenGraph(C.Structure):
+    _fields_ = [("n", C.c_int64), ("nnz", C.c_int64), ("rowptr", C.c_void_p),
+                ("col", C.c_void_p), ("val", C.c_void_p), ("wsum", C.c_double)]
+
+
+def _gen(fn, *args):
+    g = _GenGraph()
+    f = getattr(lib(), fn)
+    rc = f(*args, C.byref(g))
+    if rc != 0:
+        raise ValueError("%s failed: %d" % (fn, rc))
+    try:
+        n, nnz = g.n, g.nnz
+        rp = np.ctypeslib.as_array((C.c_int32 * (n + 1)).from_address(g.rowptr)).copy()
+        col = (np.ctypeslib.as_array((C.c_int32 * nnz).from_address(g.col)).copy()
+               if nnz else np.empty(0, np.int32))
+        val = (np.ctypeslib.as_array((C.c_double * nnz).from_address(g.val)).copy()
+               if nnz else np.empty(0))
+    finally:
+        lib().sbo_graph_free(C.byref(g))
+    return Graph(n, rp, col, val, g.wsum)
+
+
+# The engine's seeded synthetic instances (sbx.gen_*), restated in sbo_gen.c:
+# the same arguments give the same arrays.
+def gen_er(n, p, pm1=False, seed=1234):
+    return _gen("sbo_gen_er", C.c_int64(n), C.c_double(p), C.c_int(1 if pm1 else 0),
+                C.c_uint64(seed))
+
+
+def gen_torus(rows, cols, seed=1234):
+    return _gen("sbo_gen_torus", C.c_int32(rows), C.c_int32(cols), C.c_uint64(seed))
+
+
+def gen_rmat(scale, edge_factor=4, a=0.57, b=0.19, c=0.19, seed=1234):
+    return _gen("sbo_gen_rmat", C.c_int32(scale), C.c_int32(edge_factor), C.c_double(a),
+                C.c_double(b), C.c_double(c), C.c_uint64(seed))
+
+
+def gen_rgg(n, avg_degree, seed=1234):
+    return _gen("sbo_gen_rgg", C.c_int64(n), C.c_double(avg_degree), C.c_uint64(seed))
+
+
+def gen_cities(N, scale=1.0, seed=1234):
+    xc = np.empty(N)
+    yc = np.empty(N)
+    rc = lib().sbo_gen_cities(C.c_int32(N), C.c_double(scale), C.c_uint64(seed),
+                              xc.ctypes.data_as(C.c_void_p), yc.ctypes.data_as(C.c_void_p))
+    if rc != 0:
+        raise ValueError("sbo_gen_cities failed")
+    return xc, yc
+
+
+def tsp_distances(xc, yc, kind):
+    N = len(xc)
+    xc = np.ascontiguousarray(xc, np.float64)
+    yc = np.ascontiguousarray(yc, np.float64)
+    packed = np.empty(N * (N - 1) // 2)
+    if lib().sbo_tsp_distances(C.c_int32(N), xc.ctypes.data_as(C.c_void_p),
+                               yc.ctypes.data_as(C.c_void_p), C.c_int(kind),
+                               packed.ctypes.data_as(C.c_void_p)) != 0:
+        raise ValueError("bad TSP instance")
+    return packed
+
+
 def params(dt=0.1, steps=10000, agents=1024, fused=1, uw=0, period=100,
-           threshold=25, seed=1234, schedule=JACOBI, nthreads=0):
+           threshold=25, seed=1234, schedule=JACOBI, nthreads=0, run_steps=0):
     return Params(dt, steps, agents, fused, uw, period, threshold, seed, schedule,
-                  nthreads)
+                  nthreads, run_steps)
 
 
 def rand_stream(seed, count):
@@ -160,6 +225,48 @@ def maxcut_solve(g, p, want_state=False):
     out = {"result": r.as_dict(), "cut": cutv}
     if want_state:
         out.update(x=x, y=y, spins=s)
+    return out
+
+
+F32, BF16, F16 = 0, 1, 2   # the engine's lower-precision storage modes
+
+
+def round_storage(prec, v):
+    """float32 values rounded to the storage type (returned as float32)."""
+    v = np.ascontiguousarray(v, np.float32)
+    f = lib().sbo_round_storage
+    f.restype = C.c_float
+    return np.array([f(C.c_int(prec), C.c_float(float(a))) for a in v.ravel()],
+                    np.float32).reshape(v.shape)
+
+
+def init_maxcut_lp(n, A, seed, prec):
+    x = np.empty(n * A, np.float32)
+    y = np.empty(n * A, np.float32)
+    lib().sbo_init_maxcut_lp(C.c_int64(n), C.c_int64(A), C.c_uint32(seed), C.c_int(prec),
+                             x.ctypes.data_as(C.c_void_p), y.ctypes.data_as(C.c_void_p))
+    return x, y
+
+
+def maxcut_solve_lp(g, p, prec, want_state=False):
+    """The MaxCut solve in the engine's FP32 / BF16 / FP16 state mode: float
+    arithmetic in the engine's operation order, rounded to the storage type
+    on every store.  State is returned as float64 (exact)."""
+    c = g.cstruct()
+    A = p.agents
+    r = Result()
+    cutv = np.empty(A)
+    x = np.empty(g.n * A, np.float32) if want_state else None
+    y = np.empty(g.n * A, np.float32) if want_state else None
+    s = np.empty(g.n * A, np.int32) if want_state else None
+    vp = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)
+    rc = lib().sbo_maxcut_solve_lp(C.byref(c), C.byref(p), C.c_int(prec), C.byref(r), vp(cutv),
+                                   vp(x), vp(y), vp(s))
+    if rc != 0:
+        raise ValueError("sbo_maxcut_solve_lp failed: %d" % rc)
+    out = {"result": r.as_dict(), "cut": cutv}
+    if want_state:
+        out.update(x=x.astype(np.float64), y=y.astype(np.float64), spins=s)
     return out
 
 

@@ -258,7 +258,8 @@ int sbo_maxcut_solve(const sbo_csr *J, const sbo_params *p, sbo_result *r,
     int64_t hstep = 0;       /* the host step counter (Ising::step) */
     int64_t windows = 0;
     sbo_update_xy(x, y, n * A, dstep, p->steps, p->dt);   /* ising.cu:188 */
-    int run = hstep < p->steps;
+    const int64_t limit = p->run_steps > 0 && p->run_steps < p->steps ? p->run_steps : p->steps;
+    int run = hstep < limit;
     while (run) {
         for (int32_t i = 0; i < p->period; i++) {
             if (p->fused)
@@ -271,7 +272,7 @@ int sbo_maxcut_solve(const sbo_csr *J, const sbo_params *p, sbo_result *r,
         sbo_window(x, n, A, cur, fin, bif, prev, stab, p->threshold);
         windows++;
         hstep += p->period;
-        run = hstep < p->steps;
+        run = hstep < limit;
         if (p->uw) {
             int64_t nb = 0;
             for (int64_t c = 0; c < A; c++) nb += bif[c];

@@ -160,6 +160,10 @@ void sbo_tsp_step(const sbo_csr *J, const double *rowsum, double *x, double *y,
     }
     double *x0 = (double *)malloc((size_t)(n * A) * sizeof(double));
     memcpy(x0, x, (size_t)(n * A) * sizeof(double));
+    /* Jacobi: every (row, agent) reads x0 only, so rows run in parallel */
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 8)
+#endif
     for (int64_t r = 0; r < n; r++)
         for (int64_t c = 0; c < A; c++)
             tsp_thread(J, rowsum, x, y, x0, A, r, c, step, max_steps, dt, xi0,

@@ -73,6 +73,7 @@ struct sbx_ctx {
     std::set<sbx_problem *> problems;   // live problems; orphaned on destroy
     std::vector<BatchClass> batch;      // packed classes of the last batch
     std::string batch_key;
+    int batch_last = -1;                // class whose state the work buffers hold
     std::vector<TraceRec> trace;        // per-window records of the last traced solve
     // autotuned tiles by matrix shape (rows, entries, degrees, weight kind),
     // precision, agents and mode: a problem uploaded again reuses its tile
@@ -653,10 +654,10 @@ int run_stream(sbx_ctx *ctx, const void *key_obj, const SolveDims &d, const DevC
         int per_chunk = 0;
         if (use_graph) {
             char key[256];
-            snprintf(key, sizeof key, "%p/%lld/%d/%d/%d/%d/%d/%d/%d/%d/%.17g/%llu/%p/%d/%d/%d/%d/%d/%d",
+            snprintf(key, sizeof key, "%p/%lld/%d/%d/%d/%d/%d/%d/%d/%d/%.17g/%llu/%p/%d/%d/%d/%d/%d/%d/%d",
                      key_obj, (long long)d.n, d.A, d.prec, d.period, d.fused, d.uw, d.threshold,
                      (int)d.pdl, d.steps, d.c0, (unsigned long long)g_alloc_gen, (void *)s, d.tv,
-                     d.tlr, d.tbt, d.tcm, d.tst, d.trace);
+                     d.tlr, d.tbt, d.tcm, d.tst, d.trace, d.giveup);
             if (!ctx->gexec || ctx->gkey != key) {
                 if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
                 ctx->gexec = nullptr;
@@ -729,6 +730,7 @@ int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_r
     d.xi0 = xi0_of(p->J);
     d.c0 = d.dt * d.xi0;
     d.pdl = !(pr->flags & SBX_FLAG_NO_PDL);
+    d.giveup = (pr->flags & SBX_FLAG_TEST_GIVEUP) ? 1 : 0;
     d.trace = (pr->trace || pr->target > 0) ? 1 : 0;
     const bool profile = (pr->flags & SBX_FLAG_PROFILE) != 0;
     const bool use_graph = !(pr->flags & SBX_FLAG_NO_GRAPH) && !profile;
@@ -933,6 +935,7 @@ int solve_tsp(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
     CK(cudaMemcpyAsync(bif.data(), w.bif, d.A, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(ctl, w.ctl, sizeof ctl, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    if (ctl[CTL_ERR]) return fail(ctx, SBX_ERR_CUDA, "a bounded wait in the step kernel gave up");
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     // Decode and statistics, src/ising_tsp.cu:188-239 and :272-287.
@@ -1206,6 +1209,7 @@ void free_batch(sbx_ctx *ctx)
     }
     ctx->batch.clear();
     ctx->batch_key.clear();
+    ctx->batch_last = -1;
 }
 
 // Many MaxCut instances in one run per agent class: one block-diagonal
@@ -1223,6 +1227,7 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
         return fail(ctx, SBX_ERR_ARG, "batched solve: per-instance targets go in the targets array");
     if (pr->steps < 0 || pr->precision < 0 || pr->precision > 3 || pr->run_steps < 0 || pr->period < 0)
         return fail(ctx, SBX_ERR_ARG, "bad params");
+    ctx->batch_last = -1;
     std::string key;
     for (int32_t i = 0; i < count; i++) {
         const sbx_problem *p = problems[i];
@@ -1280,6 +1285,7 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
         d.uw = 0;
         d.dt = pr->dt;
         d.pdl = !(pr->flags & SBX_FLAG_NO_PDL);
+        d.giveup = (pr->flags & SBX_FLAG_TEST_GIVEUP) ? 1 : 0;
         d.trace = (pr->trace || targets) ? 2 : 0;
         const int32_t run = pr->run_steps > 0 ? std::min(pr->run_steps, pr->steps) : pr->steps;
         const int64_t nchunks = run > 0 ? (run + d.period - 1) / d.period : 0;
@@ -1335,6 +1341,8 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
             if ((rc = run_stream(ctx, &c.J, d, c.J, nchunks, profile, use_graph, &launches, &kms))) return rc;
         }
         CK(cudaEventRecord(ctx->ev1, s));
+        ctx->d = d;
+        ctx->batch_last = (int)(&c - &ctx->batch[0]);
         // per-instance best cut of every window: the first reaching the target
         std::vector<double> bt;
         std::vector<TraceRec> recs;
@@ -1350,8 +1358,11 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
         CK(cudaMemsetAsync(ctx->w.eacc, 0, sizeof(unsigned long long) * ne, s));
         CK(launch_cut_batch(d, c.J, ctx->w.Wp, ctx->w.eacc, s));
         std::vector<long long> E(ne);
+        int32_t ctl[CTL_N];
         CK(cudaMemcpyAsync(E.data(), ctx->w.eacc, sizeof(long long) * ne, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(ctl, ctx->w.ctl, sizeof ctl, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
+        if (ctl[CTL_ERR]) return fail(ctx, SBX_ERR_CUDA, "a bounded wait in the step kernel gave up");
         float ms = 0;
         CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
         total_us += ms * 1000.0;
@@ -1396,6 +1407,48 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
     }
     if (batch_time_us) *batch_time_us = total_us;
     ctx->have = false;
+    return SBX_OK;
+}
+
+float bf16_to_f(uint16_t h);
+float f16_to_f(uint16_t h);
+
+// x, y (storage values as double) and window spins of rows [row0, row0 + rows)
+// and agents [0, A) of the state in the work buffers, laid out as dims d.
+int read_state(sbx_ctx *ctx, const SolveDims &d, int64_t row0, int64_t rows, int32_t A, double *x,
+               double *y, int32_t *spins)
+{
+    const size_t es = prec_bytes(d.prec), nst = (size_t)rows * d.Ap;
+    std::vector<unsigned char> buf(nst * es);
+    for (int which = 0; which < 2; which++) {
+        double *out = which ? y : x;
+        if (!out) continue;
+        const unsigned char *src = (const unsigned char *)(which ? ctx->w.y : ctx->w.x) + (size_t)row0 * d.Ap * es;
+        CK(cudaMemcpy(buf.data(), src, nst * es, cudaMemcpyDeviceToHost));
+        for (int64_t r = 0; r < rows; r++)
+            for (int a = 0; a < A; a++) {
+                const size_t i = (size_t)r * d.Ap + a;
+                double v;
+                if (d.prec == P_F64) memcpy(&v, &buf[i * 8], 8);
+                else if (d.prec == P_F32) {
+                    float f;
+                    memcpy(&f, &buf[i * 4], 4);
+                    v = f;
+                } else {
+                    uint16_t h;
+                    memcpy(&h, &buf[i * 2], 2);
+                    v = d.prec == P_BF16 ? bf16_to_f(h) : f16_to_f(h);
+                }
+                out[(size_t)r * A + a] = v;
+            }
+    }
+    if (spins) {
+        std::vector<uint32_t> pl((size_t)rows * d.W);
+        CK(cudaMemcpy(pl.data(), ctx->w.Wp + (size_t)row0 * d.W, pl.size() * 4, cudaMemcpyDeviceToHost));
+        for (int64_t r = 0; r < rows; r++)
+            for (int a = 0; a < A; a++)
+                spins[(size_t)r * A + a] = ((pl[(size_t)r * d.W + a / 32] >> (a % 32)) & 1u) ? -1 : 1;
+    }
     return SBX_OK;
 }
 
@@ -1706,6 +1759,7 @@ int sbx_solve(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
         return fail(ctx, SBX_ERR_NOMEM, "state larger than the device");
     CK(cudaSetDevice(ctx->device));
     ctx->have = false;
+    ctx->batch_last = -1;   // the work buffers are about to be reused
     if (p->tsp && pr->target > 0) return fail(ctx, SBX_ERR_UNSUPPORTED, "target: MaxCut only");
     return p->tsp ? solve_tsp(ctx, p, pr, res, agent_values) : solve_maxcut(ctx, p, pr, res, agent_values);
 }
@@ -1714,38 +1768,22 @@ int sbx_get_state(sbx_ctx *ctx, double *x, double *y, int32_t *spins)
 {
     if (!ctx) return SBX_ERR_ARG;
     if (!ctx->have) return fail(ctx, SBX_ERR_STATE, "no solve yet");
-    const SolveDims &d = ctx->d;
-    const size_t es = prec_bytes(d.prec), nst = (size_t)d.n * d.Ap;
-    std::vector<unsigned char> buf(nst * es);
-    for (int which = 0; which < 2; which++) {
-        double *out = which ? y : x;
-        if (!out) continue;
-        CK(cudaMemcpy(buf.data(), which ? ctx->w.y : ctx->w.x, nst * es, cudaMemcpyDeviceToHost));
-        for (int64_t r = 0; r < d.n; r++)
-            for (int a = 0; a < d.A; a++) {
-                const size_t i = (size_t)r * d.Ap + a;
-                double v;
-                if (d.prec == P_F64) memcpy(&v, &buf[i * 8], 8);
-                else if (d.prec == P_F32) {
-                    float f;
-                    memcpy(&f, &buf[i * 4], 4);
-                    v = f;
-                } else {
-                    uint16_t h;
-                    memcpy(&h, &buf[i * 2], 2);
-                    v = d.prec == P_BF16 ? bf16_to_f(h) : f16_to_f(h);
-                }
-                out[(size_t)r * d.A + a] = v;
-            }
-    }
-    if (spins) {
-        std::vector<uint32_t> pl((size_t)d.n * d.W);
-        CK(cudaMemcpy(pl.data(), ctx->w.Wp, pl.size() * 4, cudaMemcpyDeviceToHost));
-        for (int64_t r = 0; r < d.n; r++)
-            for (int a = 0; a < d.A; a++)
-                spins[(size_t)r * d.A + a] = ((pl[(size_t)r * d.W + a / 32] >> (a % 32)) & 1u) ? -1 : 1;
-    }
-    return SBX_OK;
+    CK(cudaSetDevice(ctx->device));
+    return read_state(ctx, ctx->d, 0, ctx->d.n, ctx->d.A, x, y, spins);
+}
+
+int sbx_get_batch_state(sbx_ctx *ctx, int32_t index, double *x, double *y, int32_t *spins)
+{
+    if (!ctx) return SBX_ERR_ARG;
+    if (ctx->batch_last < 0 || ctx->batch_last >= (int)ctx->batch.size())
+        return fail(ctx, SBX_ERR_STATE, "no batched solve yet");
+    const BatchClass &c = ctx->batch[(size_t)ctx->batch_last];
+    for (size_t i = 0; i < c.idx.size(); i++)
+        if (c.idx[i] == index) {
+            CK(cudaSetDevice(ctx->device));
+            return read_state(ctx, ctx->d, c.row_off[i], c.probs[i]->J.n, c.agents[i], x, y, spins);
+        }
+    return fail(ctx, SBX_ERR_STATE, "instance not in the last agent class solved (its state was overwritten)");
 }
 
 int sbx_get_tours(sbx_ctx *ctx, int32_t *tours, int32_t *valid_step)

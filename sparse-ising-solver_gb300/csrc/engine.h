@@ -144,6 +144,7 @@ struct SolveDims {
     int32_t tst = 0;         // 1: whole-warp rows staged through shared memory (bulk copies)
     int trace = 0;           // per-window best-cut records: 1 one problem, 2 batched
     int32_t steps_run = 0;   // resident batch: SB steps of the run
+    int giveup = 0;          // SBX_FLAG_TEST_GIVEUP: bounded waits give up at once
 };
 
 // A batch class packed for the resident batch kernel (k_resident_batch.cu):

@@ -37,6 +37,7 @@ struct RsP {
     int32_t n, A, Ap, W, period, threshold, uw;
     int32_t step0, nsteps, first, unit;
     float c0;
+    int32_t giveup;                     // test only: the window barrier gives up at once
 };
 
 constexpr int KA = 8;   // agents per CTA: one sign byte per row
@@ -267,10 +268,13 @@ __global__ void __launch_bounds__(NT, 1) k_resident_rs(const RsP P)
                 if (tid == 0) {
                     __threadfence();
                     atomicAdd(P.gbar, 1);
-                    const int target = (int)gridDim.x * (widx + 1);
+                    // test only (giveup): a target no window reaches and a
+                    // short limit, the path of a CTA that never arrives
+                    const int target = (int)gridDim.x * (widx + 1 + P.giveup);
+                    const uint32_t limit = P.giveup ? (1u << 12) : (1u << 26);
                     uint32_t spins = 0;
                     while (atomicAdd(P.gbar, 0) < target) {
-                        if (++spins > (1u << 26)) {
+                        if (++spins > limit) {
                             atomicExch(&P.ctl[CTL_ERR], 1);
                             s_stop = 1;
                             break;
@@ -431,6 +435,7 @@ cudaError_t launch_resident_rs(const SolveDims &d, const DevCsr &J, Work &w, int
     P.first = first ? 1 : 0;
     P.unit = J.unit ? 1 : 0;
     P.c0 = (float)d.c0;
+    P.giveup = d.giveup;
     const size_t smem = rs_smem(d.n, kRsCfgs[cfg - 1]);
     const int grid = (d.A + KA - 1) / KA;
     if (d.prec == P_BF16) return launch_rs_cfg<__nv_bfloat16>(cfg - 1, P, smem, grid, s, d.pdl);

@@ -56,6 +56,7 @@ struct StepP {
     int64_t niso;                         // isolated rows left to k_iso: the last niso entries of
                                           // order, which the row items then skip
     double c0;
+    int32_t giveup;                       // test only: the staged-row wait gives up at once
 };
 
 // One step kernel launch (kind K_*, window step or not) in the precision of
@@ -197,10 +198,11 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
                  : "memory");
 }
 // Bounded wait for phase `parity` of the barrier: false when it did not
-// complete within the limit (the caller flags the error).
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+// complete within `limit` checks (the caller flags the error).
+constexpr uint32_t kMbarLimit = 1u << 22;
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t limit = kMbarLimit)
 {
-    for (uint32_t k = 0; k < (1u << 22); k++) {
+    for (uint32_t k = 0; k < limit; k++) {
         uint32_t ok;
         asm volatile("{\n\t.reg .pred p;\n\t"
                      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -761,9 +763,11 @@ __global__ void __launch_bounds__(256, BIG ? 6 : (CM ? 4 : 5)) k_row(const StepP
             }
             const int64_t rn = gn < ng ? row_of(gn) : 0;
             if (gn < ng) issue((j + 1) & 1, rn, itn);
-            if (!mbar_wait(&s_bar[wid][j & 1], (j >> 1) & 1)) {
-                // never expected: flag it, let the copy in flight land, stop
+            if (!mbar_wait(&s_bar[wid][j & 1], (j >> 1) & 1, P.giveup ? 0u : kMbarLimit)) {
+                // never expected: flag it, let the copies in flight (this
+                // stage's and the next one's) land, within the limit, stop
                 if (lane == 0) atomicExch(&P.ctl[CTL_ERR], 1);
+                mbar_wait(&s_bar[wid][j & 1], (j >> 1) & 1);
                 if (gn < ng) mbar_wait(&s_bar[wid][(j + 1) & 1], ((j + 1) >> 1) & 1);
                 break;
             }

@@ -181,6 +181,7 @@ StepP make_step(const SolveDims &d, const DevCsr &J, Work &w)
     }
     P.Ap = d.Ap;
     P.c0 = d.c0;
+    P.giveup = d.giveup;
     return P;
 }
 

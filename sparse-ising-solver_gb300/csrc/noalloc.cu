@@ -15,7 +15,10 @@
 // first call on each device should therefore come before any stream capture.
 // Every call shares the array and finds the previous call's contents in it;
 // each call rebuilds the plane it reads first, and calls that overlap on the
-// GPU (other streams, other threads) race on it.
+// GPU (other streams, other threads) race on it.  The looked-up address is
+// kept for the life of the process: after cudaDeviceReset (or anything else
+// that tears down the device's primary context) it is stale, and the entry
+// point must not be called again in that process.
 #include "../../include/sbx.h"
 
 #include <cuda_runtime.h>
@@ -97,8 +100,10 @@ extern "C" int sbx_fused_steps_noalloc(const int32_t *d_rowptr, const int32_t *d
                                        float *d_y, double dt, double xi0, int32_t step0,
                                        int32_t nsteps, int32_t max_steps, void *cuda_stream)
 {
-    if (!d_rowptr || !d_x || !d_y || n <= 0 || agents <= 0 || step0 < 0 || nsteps < 0 ||
-        max_steps <= 0)
+    // d_col and d_val are checked even when the matrix has no entries: the
+    // number of entries is on the device, out of this call's sight.
+    if (!d_rowptr || !d_col || !d_val || !d_x || !d_y || n <= 0 || agents <= 0 || step0 < 0 ||
+        nsteps < 0 || max_steps <= 0)
         return fail(SBX_ERR_ARG, "null pointer or non-positive size");
     if (agents % 32)
         return fail(SBX_ERR_ARG, "agents must be a multiple of 32 (x, y are [n][agents])");
@@ -122,22 +127,28 @@ extern "C" int sbx_fused_steps_noalloc(const int32_t *d_rowptr, const int32_t *d
         }
         planes = g_planes_addr[dev];
     }
-    cudaStream_t s = (cudaStream_t)cuda_stream;
-    const unsigned blocks = (unsigned)((n * W + 7) / 8);
+    // Each launch reports its own error (cudaLaunchKernelEx returns it), so
+    // an error left pending by the caller's earlier work is neither consumed
+    // nor blamed on this call.
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)((n * W + 7) / 8));
+    cfg.blockDim = dim3(256);
+    cfg.stream = (cudaStream_t)cuda_stream;
     uint32_t *S[2] = {planes, planes + SBX_NOALLOC_MAX_WORDS};
+    const int32_t W32 = (int32_t)W;
     // The plane the first step gathers from is rebuilt from x: nothing is
     // read that a previous call left behind.
-    k_noalloc_signs<<<blocks, 256, 0, s>>>(d_x, S[step0 & 1], n, (int32_t)W);
+    e = cudaLaunchKernelEx(&cfg, k_noalloc_signs, (const float *)d_x, S[step0 & 1], n, W32);
+    if (e != cudaSuccess) return fail(SBX_ERR_CUDA, cudaGetErrorString(e));
     const float c0 = (float)(dt * xi0);
     for (int32_t i = 0; i < nsteps; i++) {
         const int32_t k = step0 + i;
         double p = 1.025 * (double)k / max_steps;   // src/kernels.cu:225-226
         p = p < 1.0 ? p : 1.0;
-        k_noalloc_step<<<blocks, 256, 0, s>>>(d_rowptr, d_col, d_val, d_x, d_y, S[k & 1],
-                                              S[(k + 1) & 1], n, (int32_t)W, c0,
-                                              (float)(dt * (p + 1)), (float)(dt * (p - 1)));
+        e = cudaLaunchKernelEx(&cfg, k_noalloc_step, d_rowptr, d_col, d_val, d_x, d_y,
+                               (const uint32_t *)S[k & 1], S[(k + 1) & 1], n, W32, c0,
+                               (float)(dt * (p + 1)), (float)(dt * (p - 1)));
+        if (e != cudaSuccess) return fail(SBX_ERR_CUDA, cudaGetErrorString(e));
     }
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return fail(SBX_ERR_CUDA, cudaGetErrorString(e));
     return SBX_OK;
 }

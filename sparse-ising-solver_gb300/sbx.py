@@ -19,7 +19,7 @@ ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_IO, ERR_FORMAT, ERR_UNSUPPORTED, ERR_NODEVICE,
 F32, BF16, F16, F64 = 0, 1, 2, 3
 KERNEL_AUTO, KERNEL_STREAM, KERNEL_RESIDENT, KERNEL_RESIDENT_SPLIT = 0, 1, 2, 3
 DIST_EUC_2D, DIST_GEO, DIST_EUC_2D_FLOAT = 0, 1, 2
-FLAG_NO_PDL, FLAG_NO_GRAPH, FLAG_PROFILE, FLAG_NO_TUNE = 1, 2, 4, 8
+FLAG_NO_PDL, FLAG_NO_GRAPH, FLAG_PROFILE, FLAG_NO_TUNE, FLAG_TEST_GIVEUP = 1, 2, 4, 8, 16
 PRECISIONS = {"f32": F32, "bf16": BF16, "f16": F16, "f64": F64}
 NOALLOC_MAX_WORDS = 1 << 21   # SBX_NOALLOC_MAX_WORDS in include/sbx.h
 
@@ -30,7 +30,7 @@ EXPORTS = [
     "sbx_problem_destroy", "sbx_problem_info", "sbx_solve", "sbx_get_state", "sbx_get_tours",
     "sbx_get_trace", "sbx_solve_batch", "sbx_load_mtx", "sbx_load_tsplib",
     "sbx_tsp_distances", "sbx_gen_er", "sbx_gen_torus", "sbx_gen_rmat", "sbx_gen_rgg",
-    "sbx_gen_cities", "sbx_fused_steps_noalloc",
+    "sbx_gen_cities", "sbx_fused_steps_noalloc", "sbx_get_batch_state",
 ]
 
 
@@ -265,6 +265,15 @@ class Context:
         y = np.empty(n * agents)
         s = np.empty(n * agents, np.int32)
         _check("sbx_get_state", lib().sbx_get_state(self._c, _p(x), _p(y), _p(s)))
+        return x, y, s
+
+    def batch_state(self, index, n, agents):
+        """x, y, window spins of instance `index` of the last batched solve."""
+        x = np.empty(n * agents)
+        y = np.empty(n * agents)
+        s = np.empty(n * agents, np.int32)
+        _check("sbx_get_batch_state", lib().sbx_get_batch_state(self._c, C.c_int32(index), _p(x),
+                                                                _p(y), _p(s)))
         return x, y, s
 
     def trace(self, cap=1 << 16):

@@ -10,11 +10,11 @@ import sys
 from conftest import ROOT
 
 
-def _run(extra_env=None):
+def _run(extra_env=None, workload=("--workload", "er800")):
     env = dict(os.environ)
     env.update(extra_env or {})
     return subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
-                           "--workload", "er800", "--steps", "1", "--warmup", "0"],
+                           *workload, "--steps", "1", "--warmup", "0"],
                           capture_output=True, text=True, timeout=300, env=env, cwd=ROOT)
 
 
@@ -39,3 +39,21 @@ def test_reference_arm_other_ranks_exit_quietly():
     p = _run({"RANK": "1", "WORLD_SIZE": "2"})
     assert p.returncode == 0, p.stderr[-2000:]
     assert not [l for l in p.stdout.splitlines() if l.strip().startswith("{")]
+
+
+def test_reference_arm_batch_loads_no_engine_code():
+    # The default (batched) workload: its instances come from the oracle's
+    # generators, so the arm never maps the engine's library.
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--instances', '12', "
+            "'--steps', '1', '--warmup', '0']; runpy.run_path('bench.py', run_name='__main__'); "
+            "print('MAPS', open('/proc/self/maps').read().count('libsbx'))")
+    p = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300,
+                       cwd=ROOT)
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [l for l in p.stdout.splitlines() if l.strip().startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["value"] > 0
+    assert d["config"]["workload"].startswith("batch-512")
+    assert "12 instances" in d["cpu_baseline"]["sample"]
+    assert "MAPS 0" in p.stdout

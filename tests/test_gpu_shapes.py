@@ -1,0 +1,213 @@
+"""Parity at the benchmark configurations' real shapes, through the C ABI.
+
+Each case runs the configuration's own instance (the seeded generator the
+benchmark uses), agent count, dt and step schedule, for the first steps or
+windows of the run, and checks the engine against the oracle:
+
+  * FP64 state: bit-exact with the oracle's FP64 restatement of the
+    reference (x, y, window spins, cuts, steps and windows run);
+  * FP32, BF16 and FP16 state: bit-exact with the oracle's restatement of
+    the engine's arithmetic for that storage type (float arithmetic in the
+    kernels' operation order, rounded to nearest even on every store);
+  * FP32 state also within 1e-4 (normwise, relative to max |x|) of the FP64
+    trajectory over the first 100 steps -- the parity clause for FP32.
+
+Configurations: ER n=800 at 1024 agents (resident kernel); torus 100x100 at
+1024 agents (streaming kernel, and the register + shared-memory resident
+kernel with the update-window exit); R-MAT 2^20 at 256 agents (heavy rows,
+isolated rows advanced a window at a time); TSP with 30 cities at 1024
+agents; 32 instances of the 512-instance batch at 64 agents each.
+"""
+import numpy as np
+import pytest
+
+import bench
+import sbx
+from conftest import oracle_first_steps, oracle_graph
+
+pytestmark = pytest.mark.gpu
+
+TRAJ_TOL = 1e-4
+LP = {sbx.F32: 0, sbx.BF16: 1, sbx.F16: 2}
+NAME = {sbx.F32: "f32", sbx.BF16: "bf16", sbx.F16: "f16", sbx.F64: "f64"}
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = sbx.Context(0)
+    yield c
+    c.close()
+
+
+def rel_err(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-30))
+
+
+def oracle_run(oracle, og, prec, **kw):
+    """The oracle's solve of the first windows: FP64 restatement of the
+    reference, or the restatement of the engine's lower-precision mode."""
+    p = oracle.params(**kw)
+    if prec == sbx.F64:
+        return oracle.maxcut_solve(og, p, want_state=True)
+    return oracle.maxcut_solve_lp(og, p, LP[prec], want_state=True)
+
+
+def assert_same_run(r, cut, state, o, what, bifurcated=True):
+    x, y, s = state
+    assert np.array_equal(x, o["x"]), what + ": x differs"
+    assert np.array_equal(y, o["y"]), what + ": y differs"
+    assert np.array_equal(s, o["spins"]), what + ": window spins differ"
+    assert np.array_equal(cut, o["cut"]), what + ": cuts differ"
+    assert r["steps_run"] == o["result"]["steps_run"], what
+    assert r["windows_run"] == o["result"]["windows_run"], what
+    if bifurcated:
+        assert r["bifurcated"] == o["result"]["bifurcated"], what
+
+
+def solve_and_check(ctx, oracle, g, og, prec, kernel, A, seed, dt, steps, run, uw=0, period=100,
+                    fused=1):
+    prob = ctx.problem(g)
+    r, cut = ctx.solve(prob, sbx.params(dt=dt, steps=steps, run_steps=run, period=period,
+                                        agents=A, seed=seed, precision=prec, kernel=kernel,
+                                        update_window=uw, fused=fused))
+    if kernel != sbx.KERNEL_AUTO:
+        assert r["kernel_used"] == kernel
+    o = oracle_run(oracle, og, prec, dt=dt, steps=steps, agents=A, seed=seed, uw=uw,
+                   period=period, fused=fused, run_steps=run)
+    assert_same_run(r, cut, ctx.state(g.n, A), o,
+                    "%s kernel %d" % (NAME[prec], r["kernel_used"]))
+    prob.close()
+    return r
+
+
+# ---- configuration 1: ER n=800, p=0.0601, +1, 1024 agents, dt 0.1 ----
+
+@pytest.fixture(scope="module")
+def er800():
+    wl = bench.WORKLOADS["er800"]
+    return wl, bench.build_instance(wl)
+
+
+@pytest.mark.parametrize("prec", [sbx.F32, sbx.BF16])
+def test_er800_1024_agents_resident_bitexact(ctx, oracle, er800, prec):
+    wl, g = er800
+    og = oracle_graph(oracle, g)
+    solve_and_check(ctx, oracle, g, og, prec, sbx.KERNEL_RESIDENT, wl["agents"], 1, wl["dt"],
+                    wl["sb_steps"], 200)
+
+
+def test_er800_1024_agents_fp32_within_1e4_of_fp64(ctx, oracle, er800):
+    wl, g = er800
+    A, dt, steps = wl["agents"], wl["dt"], wl["sb_steps"]
+    r, _ = ctx.solve(ctx.problem(g), sbx.params(dt=dt, steps=steps, run_steps=100, agents=A,
+                                                seed=1, precision=sbx.F32,
+                                                kernel=sbx.KERNEL_RESIDENT))
+    x, y, _ = ctx.state(g.n, A)
+    ox, oy = oracle_first_steps(oracle, oracle_graph(oracle, g), A, 1, dt, steps, 100, 1)
+    assert rel_err(x, ox) < TRAJ_TOL and rel_err(y, oy) < TRAJ_TOL
+
+
+# ---- configuration 2: torus 100x100 +-1, 1024 agents, dt 0.5, update window ----
+
+@pytest.fixture(scope="module")
+def torus():
+    wl = bench.WORKLOADS["torus"]
+    return wl, bench.build_instance(wl)
+
+
+@pytest.mark.parametrize("prec,kernel", [(sbx.F64, sbx.KERNEL_STREAM), (sbx.F32, sbx.KERNEL_STREAM),
+                                         (sbx.BF16, sbx.KERNEL_STREAM),
+                                         (sbx.BF16, sbx.KERNEL_RESIDENT_SPLIT),
+                                         (sbx.F16, sbx.KERNEL_RESIDENT_SPLIT)])
+def test_torus_1024_agents_bitexact(ctx, oracle, torus, prec, kernel):
+    wl, g = torus
+    og = oracle_graph(oracle, g)
+    solve_and_check(ctx, oracle, g, og, prec, kernel, wl["agents"], 1, wl["dt"], wl["sb_steps"],
+                    300, uw=1)
+
+
+def test_torus_1024_agents_fp32_within_1e4_of_fp64(ctx, oracle, torus):
+    wl, g = torus
+    A, dt, steps = wl["agents"], wl["dt"], wl["sb_steps"]
+    ctx.solve(ctx.problem(g), sbx.params(dt=dt, steps=steps, run_steps=100, agents=A, seed=1,
+                                         precision=sbx.F32, kernel=sbx.KERNEL_STREAM,
+                                         update_window=1))
+    x, y, _ = ctx.state(g.n, A)
+    ox, oy = oracle_first_steps(oracle, oracle_graph(oracle, g), A, 1, dt, steps, 100, 1)
+    assert rel_err(x, ox) < TRAJ_TOL and rel_err(y, oy) < TRAJ_TOL
+
+
+def test_torus_bf16_to_the_update_window_exit(ctx, oracle):
+    # A 40x40 torus at 256 agents run to the all-bifurcated exit: the
+    # register + shared resident kernel's device-side exit stops at the
+    # oracle's window, with identical state.
+    g = sbx.gen_torus(40, 40, seed=1234)
+    og = oracle_graph(oracle, g)
+    r = solve_and_check(ctx, oracle, g, og, sbx.BF16, sbx.KERNEL_RESIDENT_SPLIT, 256, 3, 0.5, 20000,
+                        0, uw=1)
+    assert r["steps_run"] < 20000
+
+
+# ---- configuration 3: R-MAT 2^20, 256 agents, dt 0.5 ----
+
+@pytest.fixture(scope="module")
+def rmat20():
+    wl = bench.WORKLOADS["rmat20"]
+    return wl, bench.build_instance(wl)
+
+
+@pytest.mark.parametrize("prec", [sbx.F64, sbx.BF16])
+def test_rmat20_256_agents_first_window_bitexact(ctx, oracle, rmat20, prec):
+    # A 10-step window: the step kernel with heavy-row chunks and mixed
+    # counting, and the isolated rows' window kernel, at full size.
+    wl, g = rmat20
+    og = oracle_graph(oracle, g)
+    r = solve_and_check(ctx, oracle, g, og, prec, sbx.KERNEL_STREAM, wl["agents"], 1, wl["dt"],
+                        wl["sb_steps"], 10, period=10)
+    assert r["steps_run"] == 10
+
+
+# ---- configuration 4: TSP, 30 cities, 1024 agents, dt 0.1 ----
+
+def test_tsp30_1024_agents_fp64_bitexact(ctx, oracle):
+    wl = bench.WORKLOADS["tsp30"]
+    inst = bench.build_instance(wl)
+    N, A, steps, run = inst["N"], wl["agents"], wl["sb_steps"], 200
+    prob = ctx.tsp_problem(inst["packed"], N, A=inst["A"], B=inst["B"], C_=inst["C"])
+    r, _ = ctx.solve(prob, sbx.params(dt=wl["dt"], steps=steps, run_steps=run, period=100,
+                                      agents=A, seed=1, precision=sbx.F64))
+    assert r["steps_run"] == run
+    x, y, _ = ctx.state(N * N, A)
+    t = bench.oracle_tsp(inst)
+    ox, oy = oracle.init_tsp(N * N, A, 1)
+    oracle.update_xy(ox, oy, 0, steps, wl["dt"])
+    for k in range(run):
+        t.step(ox, oy, A, k, steps, wl["dt"])
+    assert np.array_equal(x, ox) and np.array_equal(y, oy)
+
+
+# ---- configuration 5: the batch, 32 of its 512 instances, 64 agents each ----
+
+@pytest.fixture(scope="module")
+def batch32():
+    wl = bench.WORKLOADS["batch512"]
+    specs = bench.batch_specs(wl["instances"])[::16]
+    return wl, [bench.batch_graph(sp, sbx) for sp in specs]
+
+
+@pytest.mark.parametrize("prec", [sbx.F64, sbx.BF16])
+def test_batch_subset_bitexact_per_instance(ctx, oracle, batch32, prec):
+    wl, graphs = batch32
+    A, run, seed = wl["agents"], 200, 1
+    probs = [ctx.problem(g) for g in graphs]
+    res, vals, _ = ctx.solve_batch(probs, [A] * len(probs),
+                                   sbx.params(dt=wl["dt"], steps=wl["sb_steps"], run_steps=run,
+                                              seed=seed, precision=prec))
+    for i, g in enumerate(graphs):
+        o = oracle_run(oracle, oracle_graph(oracle, g), prec, dt=wl["dt"], steps=wl["sb_steps"],
+                       agents=A, seed=seed + i, run_steps=run)
+        # (a batched solve reports no per-instance bifurcated count)
+        assert_same_run(res[i], vals[i * A:(i + 1) * A], ctx.batch_state(i, g.n, A), o,
+                        "batch instance %d (n=%d)" % (i, g.n), bifurcated=False)
+    for p in probs:
+        p.close()

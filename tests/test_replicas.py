@@ -40,6 +40,16 @@ def test_merged_statistics_equal_the_single_run():
         assert got["count"] == cuts.size
         assert abs(got["mean"] - ref["mean"]) <= 1e-12 * abs(ref["mean"])
         assert abs(got["std"] - ref["std"]) <= 1e-6 * ref["std"]
+    # large cuts with a small spread (R-MAT scale: ~2.5e6 +- tens): a merge
+    # through sums of squares cancels catastrophically, the pairwise one not
+    big = 2.5e6 + rng.integers(0, 60, size=256).astype(np.float64)
+    refb = _reference_stats(big)
+    for world in (2, 3, 8):
+        parts = [replicas.local_summary(big[o:o + c])
+                 for o, c in (replicas.agent_shard(big.size, world, r) for r in range(world))]
+        got = replicas.merge_summaries(parts)
+        assert abs(got["std"] - refb["std"]) <= 1e-9 * refb["std"]
+        assert abs(got["mean"] - refb["mean"]) <= 1e-15 * refb["mean"]
     # a rank with no agents changes nothing
     got = replicas.merge_summaries([replicas.local_summary(cuts), replicas.local_summary([])])
     assert got["max"] == ref["max"] and got["count"] == cuts.size

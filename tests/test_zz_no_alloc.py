@@ -2,7 +2,9 @@
 memory (all of it held by their own arena, or a loop that cannot take the
 synchronisation cudaMalloc may bring).  The entry point is called through the
 C ABI on buffers the caller owns; its result must match sbx_solve's, call
-after call, because it shares one static scratch array between calls.
+after call -- from odd and even steps, and on a second graph whose signs the
+array does not hold -- because it shares one static scratch array between
+calls.
 
 This file is collected last on purpose: if it fails, a run that stops at the
 first failure has already run every other test."""
@@ -63,6 +65,36 @@ def test_noalloc_steps_match_sbx_solve_on_two_calls():
         xe, ye, _ = ctx.state(g.n, A)
         assert rel(x.cpu().numpy().ravel(), xe) < TOL
         assert rel(y.cpu().numpy().ravel(), ye) < TOL
+
+    # A third call on another graph, from an even step: the planes the first
+    # two calls left in the shared array are wrong for it, and it starts on
+    # the other plane.  It must still match sbx_solve.
+    g2 = sbx.gen_er(420, 0.08, pm1=True, seed=11)
+    prob2 = ctx.problem(g2)
+    base2 = dict(base, seed=seed + 1)
+    r2, _ = ctx.solve(prob2, sbx.params(run_steps=2, **base2))
+    x2, y2, _ = ctx.state(g2.n, A)
+    rowptr2 = torch.tensor(g2.rowptr, dtype=torch.int32, device=dev)
+    col2 = torch.tensor(g2.col, dtype=torch.int32, device=dev)
+    val2 = torch.tensor(g2.val.astype(np.float32), device=dev)
+    xb = torch.tensor(x2.astype(np.float32).reshape(g2.n, A), device=dev)
+    yb = torch.tensor(y2.astype(np.float32).reshape(g2.n, A), device=dev)
+    rc = f(rowptr2.data_ptr(), col2.data_ptr(), val2.data_ptr(), g2.n, A, xb.data_ptr(),
+           yb.data_ptr(), dt, r2["xi0"], 2, 30, max_steps, stream)
+    assert rc == sbx.OK, sbx.lib().sbx_last_error()
+    torch.cuda.synchronize()
+    ctx.solve(prob2, sbx.params(run_steps=32, **base2))
+    xe, ye, _ = ctx.state(g2.n, A)
+    assert rel(xb.cpu().numpy().ravel(), xe) < TOL
+    assert rel(yb.cpu().numpy().ravel(), ye) < TOL
+
+    # a null column or value array is refused, whatever the matrix holds
+    rc = f(rowptr.data_ptr(), None, val.data_ptr(), g.n, A, x.data_ptr(), y.data_ptr(), dt,
+           r["xi0"], 0, 1, max_steps, stream)
+    assert rc == -1 and b"null pointer" in sbx.lib().sbx_last_error()
+    rc = f(rowptr.data_ptr(), col.data_ptr(), None, g.n, A, x.data_ptr(), y.data_ptr(), dt,
+           r["xi0"], 0, 1, max_steps, stream)
+    assert rc == -1 and b"null pointer" in sbx.lib().sbx_last_error()
 
     # beyond the static array: refused before any work, with the reason
     n_big = sbx.NOALLOC_MAX_WORDS + 1   # agents = 32: one word per row
