@@ -340,7 +340,8 @@ def main():
                     help="--profile: kernel family")
     ap.add_argument("--tile", default="", metavar="V,LR,BT,CM",
                     help="--profile: streaming tile (agents per lane, lanes per row, threads, "
-                         "count mode 1 bytes / 2 bit planes); default: the fixed heuristic")
+                         "count mode 1 bytes / 2 bit planes / 4 shared-memory planes, batched); "
+                         "default: the fixed heuristic")
     ap.add_argument("--legs", default="all", choices=["all", "main"],
                     help="main: only the timed solves of the main precision (profiling)")
     ap.add_argument("--instances", type=int, default=0, metavar="K",
@@ -574,7 +575,10 @@ def run_profile_case(args, wl):
               flags=sbx.FLAG_NO_GRAPH | sbx.FLAG_NO_TUNE | (sbx.FLAG_PROFILE if args.step_times else 0))
     if args.tile:
         v, lr, bt, cm = (int(t) for t in args.tile.split(","))
-        kw.update(lane_agents=v, row_lanes=lr, block_threads=bt, count_mode=cm)
+        if cm == 4:   # the shared-memory-plane batch kernel: its CTA size only
+            kw.update(block_threads=bt, count_mode=cm)
+        else:
+            kw.update(lane_agents=v, row_lanes=lr, block_threads=bt, count_mode=cm)
     ctx = sbx.Context(0)
     size = {}
     if wl["kind"] == "batch":

@@ -90,8 +90,12 @@ typedef struct sbx_params {
                                planes per sign word (neighbours split across
                                the word's lanes), 3 mixed (rows with more than
                                127 neighbours present: bit planes for rows of
-                               12 or more neighbours, byte counters below);
-                               0: autotuned */
+                               12 or more neighbours, byte counters below),
+                               4 (batched, 16-bit state, 32/64/128 agents,
+                               degree <= 127) each instance's sign plane in
+                               shared memory, a lane per 32-agent word --
+                               block_threads 512 or 1024 sets its CTA size;
+                               0: autotuned (batches that fit take 4) */
     int32_t staging;        /* state larger than L2, whole-warp rows: 1 direct
                                loads, 2 rows copied ahead into shared memory
                                (bulk asynchronous copies); 0: autotuned */

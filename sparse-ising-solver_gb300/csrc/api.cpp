@@ -52,6 +52,7 @@ struct BatchClass {
     double dt = -1;                       // dt of the uploaded per-row c0
     DevRb rb;                             // packed for the resident batch kernel (on first use)
     int64_t rb_max = 0;                   // bin capacity the packing was made for
+    DevBsm bsm;                           // plan of the shared-memory-plane step (on first use)
 };
 
 struct sbx_ctx {
@@ -657,7 +658,7 @@ int run_stream(sbx_ctx *ctx, const void *key_obj, const SolveDims &d, const DevC
             snprintf(key, sizeof key, "%p/%lld/%d/%d/%d/%d/%d/%d/%d/%d/%.17g/%llu/%p/%d/%d/%d/%d/%d/%d/%d",
                      key_obj, (long long)d.n, d.A, d.prec, d.period, d.fused, d.uw, d.threshold,
                      (int)d.pdl, d.steps, d.c0, (unsigned long long)g_alloc_gen, (void *)s, d.tv,
-                     d.tlr, d.tbt, d.tcm, d.tst, d.trace, d.giveup);
+                     d.tlr, d.tbt, d.tcm, d.tst, d.trace, d.giveup * 2 + d.tbsm);
             if (!ctx->gexec || ctx->gkey != key) {
                 if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
                 ctx->gexec = nullptr;
@@ -1106,6 +1107,100 @@ void free_rb(DevRb &B)
     B = DevRb();
 }
 
+void free_bsm(DevBsm &M)
+{
+    cudaFree(M.lcol);
+    cudaFree(M.seg);
+    cudaFree(M.cta_seg);
+    cudaFree(M.ioff);
+    cudaFree(M.in);
+    M = DevBsm();
+}
+
+// Can the class run the shared-memory-plane step kernel: 16-bit state, +-1
+// weights, at most 127 neighbours per row (seven count planes), 32, 64 or 128
+// padded agents, and the largest instance's plane fits in shared memory.
+bool bsm_ok(const BatchClass &c, const SolveDims &d)
+{
+    if (d.prec != P_BF16 && d.prec != P_F16) return false;
+    if (!c.J.unit || c.J.max_deg > kHeavy) return false;
+    if (d.W != 1 && d.W != 2 && d.W != 4) return false;
+    int64_t maxn = 0;
+    for (const sbx_problem *q : c.probs) maxn = std::max<int64_t>(maxn, q->J.n);
+    const int optin = dev_attr(cudaDevAttrMaxSharedMemoryPerBlockOptin);
+    return (int64_t)bsm_smem_bytes(maxn, d.W) + 1024 <= (int64_t)optin;
+}
+
+// The plan: columns as byte offsets into the instance's plane, and the rows
+// (in instance order) cut into one contiguous run per CTA of about equal
+// cost, each run split at instance boundaries.  A row costs its neighbours
+// plus the update of its agents (about 48 neighbour loads' worth at 64
+// agents, measured by instruction counts of the kernel's loops).
+int build_bsm(sbx_ctx *ctx, BatchClass &c, int W)
+{
+    DevBsm &M = c.bsm;
+    const int64_t n = c.J.n, nnz = c.J.nnz;
+    const size_t ni = c.probs.size();
+    std::vector<uint32_t> lcol((size_t)nnz);
+    std::vector<int32_t> ioff(ni), in(ni);
+    int64_t maxn = 0;
+    for (size_t i = 0; i < ni; i++) {
+        const int64_t r0 = c.row_off[i], rn = c.probs[i]->J.n;
+        ioff[i] = (int32_t)r0;
+        in[i] = (int32_t)rn;
+        maxn = std::max(maxn, rn);
+        for (int64_t e = c.J.hrowptr[(size_t)r0]; e < c.J.hrowptr[(size_t)(r0 + rn)]; e++) {
+            const int64_t lc = (int64_t)c.J.hcol[(size_t)e] - r0;
+            // the kernel reads the plane at this offset: it must be a row of
+            // the instance (a block-diagonal matrix guarantees it)
+            if (lc < 0 || lc >= rn) return fail(ctx, SBX_ERR_ARG, "batch: a column outside its instance");
+            lcol[(size_t)e] = (uint32_t)lc * (uint32_t)(4 * W) | (c.J.hval[(size_t)e] < 0 ? 0x80000000u : 0u);
+        }
+    }
+    const int grid = std::max(1, dev_attr(cudaDevAttrMultiProcessorCount));
+    const double row_cost = 16.0 * W + 16.0;
+    double total = 0;
+    for (int64_t r = 0; r < n; r++) total += row_cost + (c.J.hrowptr[(size_t)r + 1] - c.J.hrowptr[(size_t)r]);
+    std::vector<int32_t> seg, cta((size_t)grid + 1, 0);
+    int64_t r = 0;
+    size_t inst = 0;
+    double acc = 0;
+    for (int k = 0; k < grid; k++) {
+        cta[(size_t)k] = (int32_t)(seg.size() / 3);
+        const double goal = total * (double)(k + 1) / grid;
+        const int64_t a = r;
+        while (r < n && (k == grid - 1 || acc < goal)) {
+            acc += row_cost + (c.J.hrowptr[(size_t)r + 1] - c.J.hrowptr[(size_t)r]);
+            r++;
+        }
+        // [a, r) split at instance boundaries
+        int64_t x = a;
+        while (x < r) {
+            while (inst + 1 < ni && ioff[inst + 1] <= x) inst++;
+            const int64_t end = std::min<int64_t>(r, (int64_t)ioff[inst] + in[inst]);
+            seg.push_back((int32_t)inst);
+            seg.push_back((int32_t)x);
+            seg.push_back((int32_t)end);
+            x = end;
+        }
+    }
+    cta[(size_t)grid] = (int32_t)(seg.size() / 3);
+    free_bsm(M);
+    CK(cudaMalloc(&M.lcol, sizeof(uint32_t) * std::max<int64_t>(nnz, 1)));
+    CK(cudaMalloc(&M.seg, sizeof(int32_t) * std::max<size_t>(seg.size(), 3)));
+    CK(cudaMalloc(&M.cta_seg, sizeof(int32_t) * cta.size()));
+    CK(cudaMalloc(&M.ioff, sizeof(int32_t) * ni));
+    CK(cudaMalloc(&M.in, sizeof(int32_t) * ni));
+    if (nnz) CK(cudaMemcpy(M.lcol, lcol.data(), sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice));
+    if (!seg.empty()) CK(cudaMemcpy(M.seg, seg.data(), sizeof(int32_t) * seg.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(M.cta_seg, cta.data(), sizeof(int32_t) * cta.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(M.ioff, ioff.data(), sizeof(int32_t) * ni, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(M.in, in.data(), sizeof(int32_t) * ni, cudaMemcpyHostToDevice));
+    M.grid = grid;
+    M.max_rows = maxn;
+    return SBX_OK;
+}
+
 // Pack a class for the resident batch kernel: whole instances into bins of
 // at most max_rows rows (first-fit decreasing), the rows of a bin by
 // decreasing degree, the matrix relabelled into that slot order.
@@ -1206,6 +1301,7 @@ void free_batch(sbx_ctx *ctx)
     for (auto &c : ctx->batch) {
         free_csr(c.J);
         free_rb(c.rb);
+        free_bsm(c.bsm);
     }
     ctx->batch.clear();
     ctx->batch_key.clear();
@@ -1225,7 +1321,8 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
         return fail(ctx, SBX_ERR_UNSUPPORTED, "batched solve: update_window (per-instance exit) is not supported");
     if (pr->target > 0)
         return fail(ctx, SBX_ERR_ARG, "batched solve: per-instance targets go in the targets array");
-    if (pr->steps < 0 || pr->precision < 0 || pr->precision > 3 || pr->run_steps < 0 || pr->period < 0)
+    if (pr->steps < 0 || pr->precision < 0 || pr->precision > 3 || pr->run_steps < 0 || pr->period < 0 ||
+        pr->count_mode < 0 || pr->count_mode > 4)
         return fail(ctx, SBX_ERR_ARG, "bad params");
     ctx->batch_last = -1;
     std::string key;
@@ -1320,11 +1417,29 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
             return fail(ctx, SBX_ERR_UNSUPPORTED,
                         "batched resident kernel: fused 16-bit state, degree <= 127, instances that fit on chip");
         const bool use_rb = want_rb && rb_ok;
+        // the shared-memory-plane step kernel, unless a streaming tile or
+        // another count mode is asked for (count_mode 4 insists on it)
+        const bool bsm_threads = pr->block_threads == 512 || pr->block_threads == 1024;
+        const bool tile_pinned = pr->lane_agents || pr->row_lanes || (pr->block_threads && !bsm_threads) ||
+                                 pr->staging || (pr->count_mode && pr->count_mode != 4);
+        const bool bsm_fit = !use_rb && bsm_ok(c, d);
+        if (pr->count_mode == 4 && !bsm_fit)
+            return fail(ctx, SBX_ERR_UNSUPPORTED,
+                        "count_mode 4 (shared-memory planes): 16-bit state, +-1 weights, degree <= 127, "
+                        "32/64/128 agents and instances whose plane fits in shared memory");
+        const bool use_bsm = bsm_fit && !tile_pinned && pr->kernel != SBX_KERNEL_RESIDENT &&
+                             pr->kernel != SBX_KERNEL_RESIDENT_SPLIT;
+        c.J.bsm = nullptr;
         if (use_rb) {
             if (!c.rb.rowptr || c.rb_max != rb_rows) {
                 if ((rc = build_rb(ctx, c, rb_rows))) return rc;
             }
             if ((rc = upload_rb_c0(ctx, c, pr->dt))) return rc;
+        } else if (use_bsm) {
+            if (!c.bsm.lcol && (rc = build_bsm(ctx, c, d.W))) return rc;
+            c.J.bsm = &c.bsm;
+            d.tbsm = 1;
+            d.tbt = bsm_threads ? pr->block_threads : 1024;
         } else if (nchunks) {
             bool timed = false;
             if ((rc = pick_tile(ctx, d, c.J, pr, &timed))) return rc;
@@ -1378,7 +1493,13 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
             memset(r, 0, sizeof *r);
             r->time_to_target_us = -1;
             r->steps_to_target = -1;
-            if (!use_rb) {
+            if (d.tbsm) {
+                r->lane_agents = 32;
+                r->row_lanes = d.W;
+                r->block_threads = d.tbt;
+                r->count_mode = 4;
+                r->staging = 1;
+            } else if (!use_rb) {
                 r->lane_agents = d.tv ? d.tv : default_v(d);
                 r->row_lanes = d.tlr;
                 r->block_threads = d.tbt;
@@ -1561,7 +1682,9 @@ int sbx_destroy(sbx_ctx *ctx)
                     w.btrace, w.hcount, w.gbar};
     for (void *q : ptrs)
         if (q) cudaFree(q);
+    free_batch(ctx);   // (destroys the cached graph when a batch was packed)
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    ctx->gexec = nullptr;
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     for (auto &e : ctx->evp)
@@ -1569,7 +1692,6 @@ int sbx_destroy(sbx_ctx *ctx)
     for (auto &e : ctx->prof) cudaEventDestroy(e);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->own) cudaStreamDestroy(ctx->own);
-    free_batch(ctx);
     for (sbx_problem *p : ctx->problems) p->ctx = nullptr;   // they stay valid to destroy
     delete ctx;
     return SBX_OK;

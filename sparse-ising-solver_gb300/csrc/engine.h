@@ -41,6 +41,8 @@ inline int dev_attr(cudaDeviceAttr a)
     return v;
 }
 
+struct DevBsm;
+
 // MaxCut / QUBO matrix on the device.  colw holds the column index; when every
 // weight is +-1 ("unit"), bit 31 holds the weight's sign and no value array is
 // read by the step kernels.
@@ -77,6 +79,9 @@ struct DevCsr {
     std::vector<int32_t> hrowptr, hcol, hperm;
     // The matrix relabelled into perm order (row and column s = perm slot s),
     // built on first use by the register + shared resident kernel.
+    // Batched: the plan of the shared-memory-plane step kernel, when the
+    // solve uses it (k_batch_smem.cu)
+    const DevBsm *bsm = nullptr;
     int32_t *rs_rowptr = nullptr;
     uint32_t *rs_colw = nullptr;
     float *rs_valf = nullptr;
@@ -145,6 +150,20 @@ struct SolveDims {
     int trace = 0;           // per-window best-cut records: 1 one problem, 2 batched
     int32_t steps_run = 0;   // resident batch: SB steps of the run
     int giveup = 0;          // SBX_FLAG_TEST_GIVEUP: bounded waits give up at once
+    int tbsm = 0;            // batched: the shared-memory-plane step kernel (J.bsm)
+};
+
+// Plan of the batched step kernel with per-instance sign planes in shared
+// memory (k_batch_smem.cu): the rows cut into one contiguous run per CTA,
+// each run into segments at instance boundaries.
+struct DevBsm {
+    uint32_t *lcol = nullptr;     // per entry: local column * 4W, weight sign in bit 31
+    int32_t *seg = nullptr;       // per segment: instance, first row, end row (global rows)
+    int32_t *cta_seg = nullptr;   // per CTA: first segment; grid + 1 entries
+    int32_t *ioff = nullptr;      // per instance: first row
+    int32_t *in = nullptr;        // per instance: rows
+    int32_t grid = 0;
+    int64_t max_rows = 0;         // largest instance: the shared-memory plane's rows
 };
 
 // A batch class packed for the resident batch kernel (k_resident_batch.cu):
@@ -191,6 +210,14 @@ cudaError_t launch_trace_start(Work &w, cudaStream_t s);
 // Integer weights, block-diagonal J: eacc[instance][Ap] += s_r sum_j J_rj s_j.
 cudaError_t launch_cut_batch(const SolveDims &d, const DevCsr &J, const uint32_t *plane,
                              unsigned long long *eacc, cudaStream_t s);
+
+// Batched step with shared-memory sign planes (k_batch_smem.cu): bytes of
+// dynamic shared memory for the largest instance; one launch of a fused or
+// force + clamp step (kind K_FUSED / K_FC of k_step.cuh).
+size_t bsm_smem_bytes(int64_t max_rows, int W);
+struct StepP;
+cudaError_t launch_batch_smem(const SolveDims &d, const DevBsm &M, const StepP &P, int kind, bool win,
+                              int offset, cudaStream_t s);
 
 // Resident MaxCut kernel (k_resident.cu): returns cudaErrorInvalidValue when the
 // shape does not fit.

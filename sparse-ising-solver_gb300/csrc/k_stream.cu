@@ -188,6 +188,7 @@ StepP make_step(const SolveDims &d, const DevCsr &J, Work &w)
 cudaError_t step(const SolveDims &d, const DevCsr &J, const StepP &P, int kind, bool win,
                  int offset, cudaStream_t s)
 {
+    if (d.tbsm && J.bsm && kind != K_XY) return launch_batch_smem(d, *J.bsm, P, kind, win, offset, s);
     switch (d.prec) {
     case P_F32: return step_f32(d, J, P, kind, win, offset, s);
     case P_BF16: return step_bf16(d, J, P, kind, win, offset, s);
@@ -224,7 +225,7 @@ cudaError_t launch_chunk(const SolveDims &d, const DevCsr &J, Work &w, cudaStrea
     if (!d.fused) {
         e = step(d, J, P, K_XY, false, 0, s);
         *launches += 1;
-    } else if (J.niso) {
+    } else if (J.niso && !d.tbsm) {
         // isolated rows: the whole window in one launch, which the step
         // kernels skip (events evs[2 * period], [2 * period + 1] in profile
         // mode).  Run beside the step kernels on a second stream it was
