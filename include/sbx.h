@@ -9,6 +9,8 @@
  * It replaces the reference's class interface (Sparse-Ising-Solver):
  *   sbx_problem_csr   <- CSR(string) + CSR_GPU(CSR&)          src/csr.cuh:26-47,89-95
  *   sbx_problem_tsp   <- TSP_GPU(TSP_CPU&) + construct_matrix  src/csr.cuh:65-87
+ *   sbx_problem_tsp_cities <- the same, distances on the device
+ *                                       src/kernels.cu:404-442, tsp_gpu.cu:51-112
  *   sbx_solve (MaxCut)<- Ising::Ising + Ising::symplectic_update
  *                                                             src/csr.cuh:97-104
  *   sbx_solve (TSP)   <- Ising_TSP::Ising_TSP + symplectic_update
@@ -152,6 +154,15 @@ int sbx_problem_csr(sbx_ctx *ctx, int64_t n, int64_t nnz, const int32_t *rowptr,
  * distance weight A and the row/column penalties B, C (tsp_gpu.cu:76-112). */
 int sbx_problem_tsp(sbx_ctx *ctx, int32_t ncities, const double *packed_dist,
                     double A, double B, double C, sbx_problem **out);
+/* The same problem from city coordinates, set up on the device: the packed
+ * distances of src/kernels.cu:404-442 (kind SBX_DIST_*), the per-city sums
+ * and the largest distance of src/tsp_gpu.cu:51-68, and the QUBO of
+ * src/tsp_gpu.cu:76-112 with distance weight A and B = C = penalty_scale *
+ * the largest distance (the reference: A = 1, penalty_scale = 1).
+ * Replaces TSP_GPU(TSP_CPU&) with its distance kernels, src/csr.cuh:65-87. */
+int sbx_problem_tsp_cities(sbx_ctx *ctx, int32_t ncities, const double *xc,
+                           const double *yc, int32_t kind, double A,
+                           double penalty_scale, sbx_problem **out);
 int sbx_problem_destroy(sbx_problem *p);
 int sbx_problem_info(const sbx_problem *p, int64_t *n, int64_t *nnz,
                      int32_t *is_tsp);

@@ -53,6 +53,8 @@ struct BatchClass {
     DevRb rb;                             // packed for the resident batch kernel (on first use)
     int64_t rb_max = 0;                   // bin capacity the packing was made for
     DevBsm bsm;                           // plan of the shared-memory-plane step (on first use)
+    std::vector<int32_t> agent_off;       // instance i's cuts at [agent_off[i], agent_off[i + 1])
+    int32_t *daoff = nullptr;             // the same on the device
 };
 
 struct sbx_ctx {
@@ -93,12 +95,16 @@ int fail(sbx_ctx *c, int code, const std::string &m)
     return code;
 }
 
+// A failed call's error is also the thread's pending CUDA error; it is
+// consumed here so that it is not reported again by a later call's check.
 #define CK(call)                                                                   \
     do {                                                                           \
         cudaError_t e_ = (call);                                                   \
-        if (e_ != cudaSuccess)                                                     \
+        if (e_ != cudaSuccess) {                                                   \
+            (void)cudaGetLastError();                                              \
             return fail(ctx, e_ == cudaErrorMemoryAllocation ? SBX_ERR_NOMEM : SBX_ERR_CUDA, \
                         std::string(#call) + ": " + cudaGetErrorString(e_));       \
+        }                                                                          \
     } while (0)
 
 template <class T> cudaError_t grow(T *&p, size_t &cap, size_t count)
@@ -322,33 +328,17 @@ double xi0_of(const DevCsr &J)
     return 0.7 / (sigma * std::pow((double)J.n, 0.5));
 }
 
-// ising.cu:238-265 (MaxCut) -- the reference's loop, so the statistics are
-// bit-identical for identical per-agent values.
-void stats(const std::vector<double> &v, sbx_result *r)
+// The statistics from the device's reduction (launch_stats): min, max and
+// mean as reduced there, the standard deviation and ps finished here with
+// the reference's expressions (src/ising.cu:258-265).
+void finish_stats(const double *st, int64_t A, sbx_result *r)
 {
-    const int64_t A = (int64_t)v.size();
-    double mx = -DBL_MAX, mn = DBL_MAX, total = 0, sd = 0;
-    for (double x : v) {
-        if (x > mx) mx = x;
-        if (x < mn) mn = x;
-        total += x;
-    }
-    const double avg = total / A;
-    int64_t nmax = 0;
-    int32_t best = -1;
-    for (int64_t i = 0; i < A; i++) {
-        sd += std::pow(v[i] - avg, 2);
-        if (v[i] == mx) {
-            nmax++;
-            if (best < 0) best = (int32_t)i;
-        }
-    }
-    r->min = mn;
-    r->max = mx;
-    r->mean = avg;
-    r->std = std::pow(sd / (A - 1), 0.5);
-    r->ps = (double)nmax / A;
-    r->best_agent = best;
+    r->min = st[0];
+    r->max = st[1];
+    r->mean = st[3];
+    r->std = std::pow(st[4] / (A - 1), 0.5);
+    r->ps = st[5] / A;
+    r->best_agent = (int32_t)st[6];
 }
 
 int ensure_common(sbx_ctx *ctx, const SolveDims &d, int64_t total_steps, int32_t J_nchunks = 0)
@@ -655,10 +645,10 @@ int run_stream(sbx_ctx *ctx, const void *key_obj, const SolveDims &d, const DevC
         int per_chunk = 0;
         if (use_graph) {
             char key[256];
-            snprintf(key, sizeof key, "%p/%lld/%d/%d/%d/%d/%d/%d/%d/%d/%.17g/%llu/%p/%d/%d/%d/%d/%d/%d/%d",
+            snprintf(key, sizeof key, "%p/%lld/%d/%d/%d/%d/%d/%d/%d/%d/%.17g/%llu/%p/%d/%d/%d/%d/%d/%d/%d/%d",
                      key_obj, (long long)d.n, d.A, d.prec, d.period, d.fused, d.uw, d.threshold,
                      (int)d.pdl, d.steps, d.c0, (unsigned long long)g_alloc_gen, (void *)s, d.tv,
-                     d.tlr, d.tbt, d.tcm, d.tst, d.trace, d.giveup * 2 + d.tbsm);
+                     d.tlr, d.tbt, d.tcm, d.tst, d.trace, d.giveup, d.tbsm);
             if (!ctx->gexec || ctx->gkey != key) {
                 if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
                 ctx->gexec = nullptr;
@@ -809,10 +799,16 @@ int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_r
     CK(cudaEventRecord(ctx->ev1, s));
     const int loop_launches = launches;
     CK(launch_cut(d, p->J, ctx->w, ctx->w.Wp, s, &launches));
-    std::vector<double> cut((size_t)d.A);
+    // the statistics line on the device (src/ising.cu:238-265)
+    CK(grow(ctx->w.stats, ctx->w.cap_stats, (size_t)7));
+    CK(launch_stats(ctx->w.cut, d.A, ctx->w.stats, s));
+    launches++;
+    double st[7];
     int32_t ctl[CTL_N];
     std::vector<uint8_t> bif((size_t)d.A);
-    CK(cudaMemcpyAsync(cut.data(), ctx->w.cut, sizeof(double) * d.A, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(st, ctx->w.stats, sizeof st, cudaMemcpyDeviceToHost, s));
+    if (agent_values)
+        CK(cudaMemcpyAsync(agent_values, ctx->w.cut, sizeof(double) * d.A, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(ctl, ctx->w.ctl, sizeof ctl, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(bif.data(), ctx->w.bif, d.A, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -820,7 +816,7 @@ int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_r
     CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     if (ctl[CTL_ERR]) return fail(ctx, SBX_ERR_CUDA, "a bounded wait in the step kernel gave up");
     memset(res, 0, sizeof *res);
-    stats(cut, res);
+    finish_stats(st, d.A, res);
     res->time_us = ms * 1000.0;
     res->xi0 = d.xi0;
     res->steps_run = ctl[CTL_STEP];
@@ -845,7 +841,6 @@ int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_r
         res->kernel_ms = kernel_ms;
     }
     res->gpu_launches = launches + 1;   // + the init kernel
-    if (agent_values) memcpy(agent_values, cut.data(), sizeof(double) * d.A);
     ctx->have = true;
     ctx->last_tsp = false;
     ctx->d = d;
@@ -1043,6 +1038,10 @@ int build_class(sbx_ctx *ctx, BatchClass &c)
     CK(cudaMalloc(&c.J.iwsum, sizeof(double) * c.J.ninst));
     CK(cudaMemcpy(c.J.iagents, c.agents.data(), sizeof(int32_t) * c.J.ninst, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c.J.iwsum, c.wsum.data(), sizeof(double) * c.J.ninst, cudaMemcpyHostToDevice));
+    c.agent_off.assign(ni + 1, 0);
+    for (size_t i = 0; i < ni; i++) c.agent_off[i + 1] = c.agent_off[i] + c.agents[i];
+    CK(cudaMalloc(&c.daoff, sizeof(int32_t) * (ni + 1)));
+    CK(cudaMemcpy(c.daoff, c.agent_off.data(), sizeof(int32_t) * (ni + 1), cudaMemcpyHostToDevice));
     return SBX_OK;
 }
 
@@ -1302,6 +1301,7 @@ void free_batch(sbx_ctx *ctx)
         free_csr(c.J);
         free_rb(c.rb);
         free_bsm(c.bsm);
+        cudaFree(c.daoff);
     }
     ctx->batch.clear();
     ctx->batch_key.clear();
@@ -1438,8 +1438,7 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
         } else if (use_bsm) {
             if (!c.bsm.lcol && (rc = build_bsm(ctx, c, d.W))) return rc;
             c.J.bsm = &c.bsm;
-            d.tbsm = 1;
-            d.tbt = bsm_threads ? pr->block_threads : 1024;
+            d.tbsm = bsm_threads ? pr->block_threads : 1024;
         } else if (nchunks) {
             bool timed = false;
             if ((rc = pick_tile(ctx, d, c.J, pr, &timed))) return rc;
@@ -1472,23 +1471,27 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
         }
         CK(cudaMemsetAsync(ctx->w.eacc, 0, sizeof(unsigned long long) * ne, s));
         CK(launch_cut_batch(d, c.J, ctx->w.Wp, ctx->w.eacc, s));
-        std::vector<long long> E(ne);
+        // every instance's cuts (src/kernels.cu:383-398) and its statistics
+        // line (src/ising.cu:238-265) on the device
+        const size_t ni = c.probs.size();
+        const int64_t nvals = c.agent_off.back();
+        CK(grow(ctx->w.cut, ctx->w.cap_cut, (size_t)nvals));
+        CK(grow(ctx->w.stats, ctx->w.cap_stats, 7 * ni));
+        CK(launch_stats_batch(ctx->w.eacc, c.Ap, c.J.iagents, c.daoff, c.J.iwsum, (int32_t)ni, ctx->w.cut,
+                              ctx->w.stats, s));
+        std::vector<double> st(7 * ni), cutv(agent_values ? (size_t)nvals : 0);
         int32_t ctl[CTL_N];
-        CK(cudaMemcpyAsync(E.data(), ctx->w.eacc, sizeof(long long) * ne, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(st.data(), ctx->w.stats, sizeof(double) * st.size(), cudaMemcpyDeviceToHost, s));
+        if (agent_values)
+            CK(cudaMemcpyAsync(cutv.data(), ctx->w.cut, sizeof(double) * nvals, cudaMemcpyDeviceToHost, s));
         CK(cudaMemcpyAsync(ctl, ctx->w.ctl, sizeof ctl, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         if (ctl[CTL_ERR]) return fail(ctx, SBX_ERR_CUDA, "a bounded wait in the step kernel gave up");
         float ms = 0;
         CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
         total_us += ms * 1000.0;
-        for (size_t i = 0; i < c.probs.size(); i++) {
+        for (size_t i = 0; i < ni; i++) {
             const int gi = c.idx[i];
-            std::vector<double> cut((size_t)c.agents[i]);
-            for (int32_t a = 0; a < c.agents[i]; a++) {
-                // src/kernels.cu:383-398: -0.5 * (sum of halves - W), exact
-                const double tmp = 0.5 * (double)E[i * c.Ap + a];
-                cut[a] = -0.5 * (tmp - c.wsum[i]);
-            }
             sbx_result *r = &res[gi];
             memset(r, 0, sizeof *r);
             r->time_to_target_us = -1;
@@ -1496,7 +1499,7 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
             if (d.tbsm) {
                 r->lane_agents = 32;
                 r->row_lanes = d.W;
-                r->block_threads = d.tbt;
+                r->block_threads = d.tbsm;
                 r->count_mode = 4;
                 r->staging = 1;
             } else if (!use_rb) {
@@ -1513,7 +1516,7 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
                         r->steps_to_target = recs[k].steps;
                         break;
                     }
-            stats(cut, r);
+            finish_stats(&st[7 * i], c.agents[i], r);
             r->time_us = ms * 1000.0;
             r->xi0 = c.xi0[i];
             r->steps_run = total;
@@ -1522,8 +1525,9 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
             r->agents_per_block = use_rb ? 4 : 0;
             r->kernel_launches = launches;
             r->kernel_ms = use_rb ? (profile ? ms : 0.0) : kms;
-            r->gpu_launches = launches + 3;
-            if (agent_values) memcpy(agent_values + val_off[gi], cut.data(), sizeof(double) * c.agents[i]);
+            r->gpu_launches = launches + 4;
+            if (agent_values)
+                memcpy(agent_values + val_off[gi], &cutv[(size_t)c.agent_off[i]], sizeof(double) * c.agents[i]);
         }
     }
     if (batch_time_us) *batch_time_us = total_us;
@@ -1571,6 +1575,43 @@ int read_state(sbx_ctx *ctx, const SolveDims &d, int64_t row0, int64_t rows, int
                 spins[(size_t)r * A + a] = ((pl[(size_t)r * d.W + a / 32] >> (a % 32)) & 1u) ? -1 : 1;
     }
     return SBX_OK;
+}
+
+// The QUBO as CSR, tsp_gpu.cu:76-112 then CSR::from_matrix (row-major
+// nonzeros), for the streaming TSP kernel.
+int tsp_qubo(sbx_ctx *ctx, DevTsp &t, const double *packed)
+{
+    const int N = t.N;
+    const double A = t.A, B = t.B, C = t.C;
+    int rc = SBX_OK;
+    {
+        const int64_t m = (int64_t)N * N;
+        std::vector<int32_t> rp(m + 1, 0), col;
+        std::vector<double> val;
+        for (int i = 0; i < N; i++)
+            for (int k = 0; k < N; k++) {
+                for (int j = 0; j < N; j++)
+                    for (int l = 0; l < N; l++) {
+                        double v;
+                        const bool adj = (i == j + 1 || j == i + 1 || (i == 0 && j == N - 1) ||
+                                          (i == N - 1 && j == 0));
+                        if (i != j && k == l) v = C / 4;
+                        else if (adj && k != l) {
+                            const int c1 = std::min(k, l), c2 = std::max(k, l);
+                            v = A * packed[((2 * (int64_t)N - c1 - 3) * c1) / 2 + c2 - 1] / 8;
+                        } else if (i == j && k != l) v = B / 4;
+                        else if (i == j && k == l) v = (B + C) / 4;
+                        else v = 0;
+                        if (v != 0) {
+                            col.push_back(j * N + l);
+                            val.push_back(v);
+                        }
+                    }
+                rp[(size_t)i * N + k + 1] = (int32_t)col.size();
+            }
+        rc = upload_csr(ctx, t.qubo, m, (int64_t)col.size(), rp.data(), col.data(), val.data(), 0.0, true);
+    }
+    return rc;
 }
 
 float bf16_to_f(uint16_t h)
@@ -1679,7 +1720,7 @@ int sbx_destroy(sbx_ctx *ctx)
     void *ptrs[] = {w.x, w.y, w.x2, w.S[0], w.S[1], w.Wp, w.fin, w.chg, w.newmask, w.stab, w.bif,
                     w.prev, w.ctl, w.wincount, w.visits, w.ab, w.sched, w.eacc, w.cut, w.trace,
                     w.tours, w.valid, w.rjump, w.coef32, w.coef64, w.part, w.rinst, w.trace_t0,
-                    w.btrace, w.hcount, w.gbar};
+                    w.btrace, w.hcount, w.gbar, w.stats};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     free_batch(ctx);   // (destroys the cached graph when a batch was packed)
@@ -1782,34 +1823,69 @@ int sbx_problem_tsp(sbx_ctx *ctx, int32_t N, const double *packed, double A, dou
     if (e == cudaSuccess) e = cudaMemcpy(t.I2, I2f.data(), sizeof(float) * N, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(t.I2d, t.I2h.data(), sizeof(double) * N, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) rc = fail(ctx, SBX_ERR_CUDA, cudaGetErrorString(e));
-    // The QUBO as CSR, tsp_gpu.cu:76-112 then CSR::from_matrix (row-major
-    // nonzeros), for the streaming kernel.
+    if (!rc) rc = tsp_qubo(ctx, t, packed);
+    if (rc) {
+        cudaFree(t.D);
+        cudaFree(t.I2);
+        cudaFree(t.I2d);
+        cudaFree(t.Dd);
+        free_csr(t.qubo);
+        delete p;
+        return rc;
+    }
+    ctx->problems.insert(p);
+    *out = p;
+    return SBX_OK;
+}
+
+int sbx_problem_tsp_cities(sbx_ctx *ctx, int32_t N, const double *xc, const double *yc, int32_t kind, double A,
+                           double penalty_scale, sbx_problem **out)
+{
+    if (!ctx || !out || !xc || !yc) return fail(ctx, SBX_ERR_ARG, "null argument");
+    if (N < 2 || N > 4096) return fail(ctx, SBX_ERR_ARG, "TSP: need 2 <= N <= 4096 cities");
+    if (kind < 0 || kind > 2 || !(penalty_scale > 0)) return fail(ctx, SBX_ERR_ARG, "TSP: bad distance kind or scale");
+    CK(cudaSetDevice(ctx->device));
+    sbx_problem *p = new sbx_problem;
+    p->ctx = ctx;
+    p->tsp = true;
+    DevTsp &t = p->T;
+    t.N = N;
+    t.A = A;
+    const int64_t nd = (int64_t)N * (N - 1) / 2;
+    double *dx = nullptr, *dy = nullptr, *dp = nullptr, *dmx = nullptr, *drs = nullptr;
+    std::vector<double> packed((size_t)nd), rowsum((size_t)N), I2d((size_t)N);
+    double mx = 0;
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaMalloc(&t.D, sizeof(float) * N * N);
+    if (e == cudaSuccess) e = cudaMalloc(&t.I2, sizeof(float) * N);
+    if (e == cudaSuccess) e = cudaMalloc(&t.I2d, sizeof(double) * N);
+    if (e == cudaSuccess) e = cudaMalloc(&t.Dd, sizeof(double) * N * N);
+    if (e == cudaSuccess) e = cudaMalloc(&dx, sizeof(double) * N);
+    if (e == cudaSuccess) e = cudaMalloc(&dy, sizeof(double) * N);
+    if (e == cudaSuccess) e = cudaMalloc(&dp, sizeof(double) * nd);
+    if (e == cudaSuccess) e = cudaMalloc(&dmx, sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&drs, sizeof(double) * N);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dx, xc, sizeof(double) * N, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dy, yc, sizeof(double) * N, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launch_tsp_setup(dx, dy, N, kind, A, penalty_scale, dp, dmx, drs, t, s);
+    // the packed distances come back for the CSR form of the QUBO
+    if (e == cudaSuccess) e = cudaMemcpyAsync(packed.data(), dp, sizeof(double) * nd, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&mx, dmx, sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rowsum.data(), drs, sizeof(double) * N, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(I2d.data(), t.I2d, sizeof(double) * N, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(dx);
+    cudaFree(dy);
+    cudaFree(dp);
+    cudaFree(dmx);
+    cudaFree(drs);
+    int rc = e == cudaSuccess ? SBX_OK : fail(ctx, SBX_ERR_CUDA, cudaGetErrorString(e));
     if (!rc) {
-        const int64_t m = (int64_t)N * N;
-        std::vector<int32_t> rp(m + 1, 0), col;
-        std::vector<double> val;
-        for (int i = 0; i < N; i++)
-            for (int k = 0; k < N; k++) {
-                for (int j = 0; j < N; j++)
-                    for (int l = 0; l < N; l++) {
-                        double v;
-                        const bool adj = (i == j + 1 || j == i + 1 || (i == 0 && j == N - 1) ||
-                                          (i == N - 1 && j == 0));
-                        if (i != j && k == l) v = C / 4;
-                        else if (adj && k != l) {
-                            const int c1 = std::min(k, l), c2 = std::max(k, l);
-                            v = A * packed[((2 * (int64_t)N - c1 - 3) * c1) / 2 + c2 - 1] / 8;
-                        } else if (i == j && k != l) v = B / 4;
-                        else if (i == j && k == l) v = (B + C) / 4;
-                        else v = 0;
-                        if (v != 0) {
-                            col.push_back(j * N + l);
-                            val.push_back(v);
-                        }
-                    }
-                rp[(size_t)i * N + k + 1] = (int32_t)col.size();
-            }
-        rc = upload_csr(ctx, t.qubo, m, (int64_t)col.size(), rp.data(), col.data(), val.data(), 0.0, true);
+        t.B = t.C = penalty_scale * mx;
+        t.packed = packed;
+        t.rowsum = rowsum;
+        t.I2h = I2d;
+        rc = tsp_qubo(ctx, t, packed.data());
     }
     if (rc) {
         cudaFree(t.D);
@@ -1824,6 +1900,8 @@ int sbx_problem_tsp(sbx_ctx *ctx, int32_t N, const double *packed, double A, dou
     *out = p;
     return SBX_OK;
 }
+
+
 
 int sbx_problem_destroy(sbx_problem *p)
 {

@@ -117,6 +117,7 @@ struct Work {
     int32_t *gbar = nullptr;              // window barrier of co-resident launches
     unsigned long long *eacc = nullptr;   // per-agent cut accumulators
     double *cut = nullptr;                // per-agent cuts
+    double *stats = nullptr;              // k_stats output, 7 per problem
     TraceRec *trace = nullptr;            // per-window records; trace_t0: loop start
     long long *trace_t0 = nullptr;
     double *btrace = nullptr;             // batched: best cut [window][instance]
@@ -128,7 +129,7 @@ struct Work {
     size_t cap_x = 0, cap_y = 0, cap_x2 = 0, cap_S0 = 0, cap_S1 = 0, cap_Wp = 0, cap_fin = 0,
            cap_chg = 0, cap_new = 0, cap_stab = 0, cap_bif = 0, cap_prev = 0, cap_ctl = 0,
            cap_win = 0, cap_visits = 0, cap_ab = 0, cap_sched = 0, cap_eacc = 0, cap_cut = 0,
-           cap_trace = 0, cap_t0 = 0, cap_btrace = 0, cap_tours = 0, cap_valid = 0, cap_rj = 0, cap_c32 = 0, cap_c64 = 0, cap_part = 0, cap_rinst = 0, cap_hcount = 0, cap_gbar = 0;
+           cap_trace = 0, cap_t0 = 0, cap_btrace = 0, cap_tours = 0, cap_valid = 0, cap_rj = 0, cap_c32 = 0, cap_c64 = 0, cap_part = 0, cap_rinst = 0, cap_hcount = 0, cap_gbar = 0, cap_stats = 0;
     bool rjump_ready = false;
 };
 
@@ -150,7 +151,8 @@ struct SolveDims {
     int trace = 0;           // per-window best-cut records: 1 one problem, 2 batched
     int32_t steps_run = 0;   // resident batch: SB steps of the run
     int giveup = 0;          // SBX_FLAG_TEST_GIVEUP: bounded waits give up at once
-    int tbsm = 0;            // batched: the shared-memory-plane step kernel (J.bsm)
+    int tbsm = 0;            // batched: the shared-memory-plane step kernel (J.bsm),
+                             // its CTA size (512 or 1024); 0: not used
 };
 
 // Plan of the batched step kernel with per-instance sign planes in shared
@@ -207,6 +209,15 @@ cudaError_t launch_cut(const SolveDims &d, const DevCsr &J, Work &w, const uint3
 cudaError_t launch_plain_steps(const SolveDims &d, const DevCsr &J, Work &w, int count, cudaStream_t s);
 // Traced solves: stamp the loop start on the device clock.
 cudaError_t launch_trace_start(Work &w, cudaStream_t s);
+// The statistics of src/ising.cu:238-265 on the device (k_stats): out[7] =
+// min, max, total and mean (agent order), sum of squared deviations (agent
+// order), agents at the maximum, first agent at the maximum.
+cudaError_t launch_stats(const double *v, int32_t A, double *out, cudaStream_t s);
+// Batched: cut[agent_off[i] + a] from instance i's exact sums, and out[7 i..]
+// its statistics.
+cudaError_t launch_stats_batch(const unsigned long long *eacc, int32_t Ap, const int32_t *agents,
+                               const int32_t *agent_off, const double *wsum, int32_t ninst, double *cut,
+                               double *out, cudaStream_t s);
 // Integer weights, block-diagonal J: eacc[instance][Ap] += s_r sum_j J_rj s_j.
 cudaError_t launch_cut_batch(const SolveDims &d, const DevCsr &J, const uint32_t *plane,
                              unsigned long long *eacc, cudaStream_t s);
@@ -255,6 +266,12 @@ cudaError_t launch_tsp_resident(const SolveDims &d, const DevTsp &t, Work &w, in
                                 cudaStream_t s);
 cudaError_t launch_tsp_stream(const SolveDims &d, const DevTsp &t, Work &w, cudaStream_t s,
                               int *launches);
+// TSP setup on the device from city coordinates (device xc, yc): packed
+// distances (src/kernels.cu:404-442), the tables t.D / t.Dd, the largest
+// distance *mx, per-city sums (src/tsp_gpu.cu:51-68) and the linear field
+// t.I2d / t.I2 with B = C = scale * max distance.
+cudaError_t launch_tsp_setup(const double *xc, const double *yc, int32_t N, int32_t kind, double A, double scale,
+                             double *packed, double *mx, double *rowsum, DevTsp &t, cudaStream_t s);
 // Tour length of every agent holding a valid tour (NaN otherwise) into len[A].
 cudaError_t launch_tsp_lengths(const DevTsp &t, const int32_t *tours, const int32_t *valid, int32_t A,
                                double *len, cudaStream_t s);

@@ -256,7 +256,7 @@ cudaError_t launch_batch_smem(const SolveDims &d, const DevBsm &M, const StepP &
     B.ioff = M.ioff;
     B.in = M.in;
     const size_t smem = bsm_smem_bytes(M.max_rows, d.W);
-    const int nt = d.tbt == 512 ? 512 : 1024;
+    const int nt = d.tbsm == 512 ? 512 : 1024;
     if (d.prec == P_BF16) return launch_k<__nv_bfloat16>(kind, win, d.W, P, B, M.grid, smem, offset, s, d.pdl, nt);
     if (d.prec == P_F16) return launch_k<__half>(kind, win, d.W, P, B, M.grid, smem, offset, s, d.pdl, nt);
     return cudaErrorInvalidValue;

@@ -3,6 +3,8 @@
 // bookkeeping kernels and the exact cut.
 #include "k_step.cuh"
 
+#include <cfloat>
+
 namespace sbx {
 
 namespace {
@@ -404,7 +406,98 @@ __global__ void k_cut_ordered(const int32_t *__restrict__ rowptr, const uint32_t
     cut[a] = __dmul_rn(-0.5, __dsub_rn(tmp, wsum));
 }
 
+// The statistics line of src/ising.cu:238-265 over the A values v[i] = val(i),
+// one warp: min and max (exact in any order) across the lanes; the total and
+// the sum of squared deviations from the mean in agent order by one lane, as
+// the reference's loop adds them; the agents at the maximum and the first of
+// them.  out: min, max, total, mean, sum of squared deviations, agents at max,
+// first agent at max.  The host takes the standard deviation
+// pow(sd / (A - 1), 0.5) and ps = n_max / A from these.
+template <class F>
+__device__ __forceinline__ void stats_warp(F val, int32_t A, double *out)
+{
+    const int lane = threadIdx.x & 31;
+    double mn = DBL_MAX, mx = -DBL_MAX;
+    for (int32_t i = lane; i < A; i += 32) {
+        const double v = val(i);
+        mn = fmin(mn, v);
+        mx = fmax(mx, v);
+    }
+    for (int o = 16; o; o >>= 1) {
+        mn = fmin(mn, __shfl_xor_sync(FULL, mn, o));
+        mx = fmax(mx, __shfl_xor_sync(FULL, mx, o));
+    }
+    int32_t nmax = 0, first = INT32_MAX;
+    for (int32_t i = lane; i < A; i += 32)
+        if (val(i) == mx) {
+            nmax++;
+            first = min(first, i);
+        }
+    nmax = __reduce_add_sync(FULL, nmax);
+    first = __reduce_min_sync(FULL, first);
+    if (lane == 0) {
+        double total = 0;
+#pragma unroll 8
+        for (int32_t i = 0; i < A; i++) total = __dadd_rn(total, val(i));
+        const double avg = __ddiv_rn(total, (double)A);
+        double sd = 0;
+#pragma unroll 8
+        for (int32_t i = 0; i < A; i++) {
+            const double dv = __dsub_rn(val(i), avg);
+            sd = __dadd_rn(sd, __dmul_rn(dv, dv));
+        }
+        out[0] = mn;
+        out[1] = mx;
+        out[2] = total;
+        out[3] = avg;
+        out[4] = sd;
+        out[5] = (double)nmax;
+        out[6] = (double)(first == INT32_MAX ? -1 : first);
+    }
+}
+
+__global__ void __launch_bounds__(32) k_stats(const double *__restrict__ v, int32_t A, double *out)
+{
+    stats_warp([&](int32_t i) { return v[i]; }, A, out);
+}
+
+// Batched: block i converts instance i's exact sums to cuts (src/kernels.cu:
+// 383-398, as k_cut_finish), writes them to cut[off_i ...] and its statistics
+// to out[7 i ...].
+__global__ void __launch_bounds__(32) k_stats_batch(const unsigned long long *__restrict__ eacc, int32_t Ap,
+                                                    const int32_t *__restrict__ agents,
+                                                    const int32_t *__restrict__ agent_off,
+                                                    const double *__restrict__ wsum, double *cut,
+                                                    double *out)
+{
+    const int i = blockIdx.x;
+    const int32_t A = agents[i];
+    const double W = wsum[i];
+    const unsigned long long *e = eacc + (int64_t)i * Ap;
+    double *c = cut + agent_off[i];
+    for (int32_t a = threadIdx.x; a < A; a += 32) {
+        const double tmp = 0.5 * (double)(long long)e[a];
+        c[a] = __dmul_rn(-0.5, __dsub_rn(tmp, W));
+    }
+    __syncwarp();
+    stats_warp([&](int32_t a) { return c[a]; }, A, out + 7 * (int64_t)i);
+}
+
 }  // namespace
+
+cudaError_t launch_stats(const double *v, int32_t A, double *out, cudaStream_t s)
+{
+    k_stats<<<1, 32, 0, s>>>(v, A, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stats_batch(const unsigned long long *eacc, int32_t Ap, const int32_t *agents,
+                               const int32_t *agent_off, const double *wsum, int32_t ninst, double *cut,
+                               double *out, cudaStream_t s)
+{
+    k_stats_batch<<<ninst, 32, 0, s>>>(eacc, Ap, agents, agent_off, wsum, cut, out);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_cut_batch(const SolveDims &d, const DevCsr &J, const uint32_t *plane,
                              unsigned long long *eacc, cudaStream_t s)

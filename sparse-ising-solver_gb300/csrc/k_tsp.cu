@@ -551,6 +551,88 @@ __global__ void __launch_bounds__(128) k_tsp_lengths(const int32_t *__restrict__
 
 }  // namespace
 
+namespace {
+
+// TSP_distances_EUC_2D / TSP_distances_GEO (src/kernels.cu:404-442) on the
+// device, one thread per pair c1 < c2, with the reference's expressions and
+// its (int) truncation (none for the float kind); the packed upper triangle,
+// and the symmetric N x N tables of the TSP kernels (float and FP64).
+__global__ void __launch_bounds__(256) k_tsp_dist(const double *__restrict__ xc, const double *__restrict__ yc,
+                                                  int32_t N, int32_t kind, double *packed, float *D, double *Dd)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)N * N) return;
+    const int c1 = (int)(t / N), c2 = (int)(t - (int64_t)c1 * N);
+    if (c2 <= c1) return;
+    double d;
+    if (kind == 1) {   // GEO, kernels.cu:425-441
+        const double R = 6378.388;
+        const double q1 = cos(yc[c1] - yc[c2]);
+        const double q2 = cos(xc[c1] - xc[c2]);
+        const double q3 = cos(xc[c1] + xc[c2]);
+        d = (double)(int)(R * acos(0.5 * ((1.0 + q1) * q2 - (1.0 - q1) * q3)) + 1.0);
+    } else {           // EUC_2D, kernels.cu:404-423
+        const double xd = xc[c1] - xc[c2], yd = yc[c1] - yc[c2];
+        d = pow(xd * xd + yd * yd, 0.5);
+        if (kind == 0) d = (double)(int)d;
+    }
+    packed[(int64_t)c2 + (int64_t)c1 * N - (int64_t)(c1 + 2) * (c1 + 1) / 2] = d;
+    D[(int64_t)c1 * N + c2] = D[(int64_t)c2 * N + c1] = (float)d;
+    Dd[(int64_t)c1 * N + c2] = Dd[(int64_t)c2 * N + c1] = d;
+}
+
+// The largest distance (exact in any order).
+__global__ void __launch_bounds__(256) k_tsp_max(const double *__restrict__ packed, int64_t nd, double *mx)
+{
+    double m = 0;
+    for (int64_t k = threadIdx.x; k < nd; k += blockDim.x) m = fmax(m, packed[k]);
+    for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(FULL, m, o));
+    __shared__ double w[8];
+    if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < (int)(blockDim.x >> 5); i++) m = fmax(m, w[i]);
+        *mx = fmax(m, w[0]);
+    }
+}
+
+// Per-city distance sums (src/tsp_gpu.cu:51-68 adds each pair to both of its
+// cities walking the packed array, so city c receives its pairs in ascending
+// order of the other city), then the linear field of src/kernels.cu:591-592,
+// -1 (A rowsum + (N - 2)(B + C)) / 2 with B = C = scale * max distance,
+// rounded per operation as the host states it.
+__global__ void __launch_bounds__(128) k_tsp_rows(const double *__restrict__ Dd, int32_t N, double A,
+                                                  double scale, const double *__restrict__ mx,
+                                                  double *rowsum, double *I2d, float *I2)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    double r = 0;
+    for (int k = 0; k < N; k++)
+        if (k != c) r = __dadd_rn(r, Dd[(int64_t)c * N + k]);
+    rowsum[c] = r;
+    const double B = __dmul_rn(scale, *mx);
+    const double v = __ddiv_rn(__dmul_rn(-1.0, __dadd_rn(__dmul_rn(A, r), __dmul_rn((double)(N - 2), __dadd_rn(B, B)))),
+                               2.0);
+    I2d[c] = v;
+    I2[c] = (float)v;
+}
+
+}  // namespace
+
+cudaError_t launch_tsp_setup(const double *xc, const double *yc, int32_t N, int32_t kind, double A, double scale,
+                             double *packed, double *mx, double *rowsum, DevTsp &t, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(t.D, 0, sizeof(float) * N * N, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(t.Dd, 0, sizeof(double) * N * N, s);
+    if (e != cudaSuccess) return e;
+    const int64_t nn = (int64_t)N * N;
+    k_tsp_dist<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(xc, yc, N, kind, packed, t.D, t.Dd);
+    k_tsp_max<<<1, 256, 0, s>>>(packed, (int64_t)N * (N - 1) / 2, mx);
+    k_tsp_rows<<<(N + 127) / 128, 128, 0, s>>>(t.Dd, N, A, scale, mx, rowsum, t.I2d, t.I2);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_tsp_lengths(const DevTsp &t, const int32_t *tours, const int32_t *valid, int32_t A,
                                double *len, cudaStream_t s)
 {

@@ -31,6 +31,7 @@ EXPORTS = [
     "sbx_get_trace", "sbx_solve_batch", "sbx_load_mtx", "sbx_load_tsplib",
     "sbx_tsp_distances", "sbx_gen_er", "sbx_gen_torus", "sbx_gen_rmat", "sbx_gen_rgg",
     "sbx_gen_cities", "sbx_fused_steps_noalloc", "sbx_get_batch_state",
+    "sbx_problem_tsp_cities",
 ]
 
 
@@ -240,6 +241,17 @@ class Context:
             self._c, C.c_int32(N), _p(packed), C.c_double(A), C.c_double(B), C.c_double(C_),
             C.byref(p)))
         return Problem(self, p, N * N, True, N=N, packed=packed)
+
+    def tsp_problem_cities(self, xc, yc, kind, A=1.0, penalty_scale=1.0):
+        """TSP problem from city coordinates, distances computed on the device."""
+        xc = np.ascontiguousarray(xc, np.float64)
+        yc = np.ascontiguousarray(yc, np.float64)
+        N = int(xc.size)
+        p = C.c_void_p()
+        _check("sbx_problem_tsp_cities", lib().sbx_problem_tsp_cities(
+            self._c, C.c_int32(N), _p(xc), _p(yc), C.c_int32(kind), C.c_double(A),
+            C.c_double(penalty_scale), C.byref(p)))
+        return Problem(self, p, N * N, True, N=N)
 
     def solve(self, prob, prm, want_values=True):
         r = Result()

@@ -229,6 +229,54 @@ def test_fp64_tsp_bitexact_with_reference_fixture(ctx, oracle, name):
     assert r["steps_run"] == int(ref["steps_run"][0])
 
 
+@pytest.mark.parametrize("name", TSP_CASES)
+def test_fp64_tsp_from_cities_on_device_bitexact(ctx, oracle, name):
+    # distances, per-city sums, the largest distance and the linear field
+    # computed on the device from the coordinates: the same run as the
+    # reference's fixture, bit for bit
+    ref = golden(name)
+    xc, yc, kind = sbx.load_tsplib(os.path.join(GOLDEN, str(ref["source"])))
+    N, A = len(xc), int(ref["agents"])
+    prob = ctx.tsp_problem_cities(xc, yc, kind)
+    r, lengths = ctx.solve(prob, sbx.params(dt=0.1, steps=int(ref["steps"]), agents=A,
+                                            seed=int(ref["seed"]), precision=sbx.F64,
+                                            kernel=sbx.KERNEL_STREAM))
+    x, y, _ = ctx.state(N * N, A)
+    np.testing.assert_array_equal(x, ref["x"])
+    np.testing.assert_array_equal(y, ref["y"])
+    tours, valid = ctx.tours(N, A)
+    np.testing.assert_array_equal(valid, ref["valid"])
+    t = oracle.Tsp(xc, yc, kind)
+    for a in range(A):
+        if ref["valid"][a] > 0:
+            assert lengths[a] == t.tour_length(tours[a])
+
+
+def test_tsp_cities_float_kind_with_penalty_scale(ctx, oracle):
+    # the benchmark's TSP instance kind: float distances, B = C = 1.5 max d;
+    # the device-built problem runs as the host-built one (FP32 structured
+    # kernel), tours decoded exactly
+    xc, yc = sbx.gen_cities(30, 1000.0, seed=1234)
+    packed = sbx.tsp_distances(xc, yc, sbx.DIST_EUC_2D_FLOAT)
+    mx = float(packed.max())
+    ph = ctx.tsp_problem(packed, 30, A=1.0, B=1.5 * mx, C_=1.5 * mx)
+    pd = ctx.tsp_problem_cities(xc, yc, sbx.DIST_EUC_2D_FLOAT, A=1.0, penalty_scale=1.5)
+    prm = sbx.params(dt=0.1, steps=2000, agents=256, seed=5, precision=sbx.F32)
+    rh, lh = ctx.solve(ph, prm)
+    xh, yh, _ = ctx.state(900, 256)
+    rd, ld = ctx.solve(pd, prm)
+    xd, yd, _ = ctx.state(900, 256)
+    # float distances: the device's pow may differ from the host's in the
+    # last bit, so the runs agree closely rather than bit for bit
+    assert abs(rd["valid"] - rh["valid"]) <= max(3, rh["valid"] // 10)
+    tours, valid = ctx.tours(30, 256)
+    t = oracle.Tsp(xc, yc, oracle.DIST_EUC_2D_FLOAT, A=1.0, B=1.5 * mx, C_=1.5 * mx)
+    for a in range(256):
+        if valid[a] > 0:
+            assert sorted(tours[a].tolist()) == list(range(30))
+            assert abs(ld[a] - t.tour_length(tours[a])) <= 1e-9 * t.tour_length(tours[a])
+
+
 def _tsp_f32_restatement(t, A, seed, max_steps, k):
     """The reference TSP step (src/kernels.cu:561-597) in plain float32 numpy
     with a dense J: what FP32 arithmetic alone does to the FP64 trajectory."""
@@ -336,3 +384,22 @@ def test_batch_matches_single_solves(ctx, prec):
         assert res[i]["max"] == r1["max"] and res[i]["xi0"] == r1["xi0"]
         off += a
     assert t_us > 0
+
+
+@pytest.mark.parametrize("agents", [1, 37, 5000])
+def test_statistics_line_bit_identical(ctx, oracle, agents):
+    # min, max, mean, std, ps (src/ising.cu:238-265) reduced on the device,
+    # sums in agent order: equal bit for bit to the reference's host loop
+    g = sbx.gen_er(120, 0.08, pm1=True, seed=21)
+    r, cut = ctx.solve(ctx.problem(g), sbx.params(dt=0.3, steps=400, agents=agents, seed=5,
+                                                  precision=sbx.F64, kernel=sbx.KERNEL_STREAM))
+    o = oracle.maxcut_solve(oracle_graph(oracle, g),
+                            oracle.params(dt=0.3, steps=400, agents=agents, seed=5))
+    np.testing.assert_array_equal(cut, o["cut"])
+    for k in ("min", "max", "mean", "ps"):
+        assert r[k] == o["result"][k], k
+    if agents > 1:
+        assert r["std"] == o["result"]["std"]
+    else:
+        assert np.isnan(r["std"]) and np.isnan(o["result"]["std"])
+    assert r["best_agent"] == int(np.argmax(cut))
