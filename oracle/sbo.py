@@ -380,3 +380,50 @@ class Tsp:
         if want_state:
             out.update(x=x, y=y)
         return out
+
+
+# ---- the reference's own CUDA kernels on the GPU (test infrastructure) ----
+# oracle/_ref/ref_kernels.ptx is the reference's src/kernels.cu compiled to
+# PTX where the reference sources are; oracle/_ref/libref_gpu.so
+# (oracle/ref/ref_gpu.cpp) loads it and drives the kernels as
+# src/ising.cu:85-271 does.
+REF_PTX = os.path.join(HERE, "_ref", "ref_kernels.ptx")
+REF_GPU_LIB = os.path.join(HERE, "_ref", "libref_gpu.so")
+_ref_gpu = None
+
+
+def ref_gpu_available():
+    return os.path.exists(REF_PTX) and os.path.exists(REF_GPU_LIB)
+
+
+def _ref_lib():
+    global _ref_gpu
+    if _ref_gpu is None:
+        _ref_gpu = C.CDLL(REF_GPU_LIB)
+        _ref_gpu.ref_gpu_last_error.restype = C.c_char_p
+    return _ref_gpu
+
+
+def ref_gpu_maxcut(g, agents, steps, dt, seed, uw=0, fused=1, run_windows=0, want_state=False,
+                   device=0):
+    """One MaxCut run of the reference's GPU path (its kernels, its launch
+    shapes, its graph of 100 steps + window).  Returns the statistics line
+    (time_us is the reference's own host-clock region), the per-agent cuts,
+    and x, y when asked."""
+    st = np.zeros(8)
+    cut = np.empty(agents)
+    x = np.empty(g.n * agents) if want_state else None
+    y = np.empty(g.n * agents) if want_state else None
+    vp = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)
+    rc = _ref_lib().ref_gpu_maxcut(REF_PTX.encode(), C.c_int(device), C.c_int64(g.n),
+                                   C.c_int64(g.nnz), vp(g.rowptr), vp(g.col), vp(g.val),
+                                   C.c_double(g.wsum), C.c_int(agents), C.c_int(steps),
+                                   C.c_double(dt), C.c_uint(seed), C.c_int(uw), C.c_int(fused),
+                                   C.c_int(run_windows), vp(st), vp(x), vp(y), vp(cut))
+    if rc != 0:
+        raise RuntimeError("ref_gpu_maxcut: " + _ref_lib().ref_gpu_last_error().decode())
+    out = {"time_us": st[0], "min": st[1], "max": st[2], "mean": st[3], "std": st[4],
+           "ps": st[5], "steps_run": int(st[6]), "windows_run": int(st[7]), "cut": cut}
+    if want_state:
+        out.update(x=x, y=y)
+    return out

@@ -686,7 +686,7 @@ int run_stream(sbx_ctx *ctx, const void *key_obj, const SolveDims &d, const DevC
                     CK(cudaStreamSynchronize(s));
                     // the step kernels, and the isolated rows' window kernel
                     for (int i = 0; i <= d.period; i++) {
-                        if (i == d.period && !(d.fused && J.niso)) break;
+                        if (i == d.period && !(d.fused && J.niso && !d.tbsm)) break;
                         float t = 0;
                         CK(cudaEventElapsedTime(&t, evs[2 * i], evs[2 * i + 1]));
                         kernel_ms += t;
