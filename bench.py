@@ -277,6 +277,32 @@ def cpu_batch_sample(wl, graphs, seconds=10.0, cores=0):
     return sum(g.nnz for g in graphs) * A * s / sec, cores, s, sec
 
 
+def reference_gpu_batch(wl, graphs, seed, every=16):
+    """The reference's own kernels on this GPU (oracle/_ref, where they were
+    compiled) on every `every`-th instance of the batch, one after another as
+    its CLI would run them, full runs: their nnz*agent*steps/s and best cuts.
+    None where the reference's kernels were not compiled."""
+    import numpy as np
+    import sbo
+    if not sbo.ref_gpu_available():
+        return None
+    t_us, units, best = 0.0, 0, []
+    for i in range(0, len(graphs), every):
+        g = graphs[i]
+        og = sbo.Graph(g.n, g.rowptr, g.col, g.val, g.wsum)
+        r = sbo.ref_gpu_maxcut(og, wl["agents"], wl["sb_steps"], wl["dt"], seed + i,
+                               fused=wl["fused"])
+        t_us += r["time_us"]
+        units += g.nnz * wl["agents"] * r["steps_run"]
+        best.append(r["max"])
+    return {"value": units / (t_us / 1e6), "unit": "nnz*agent*steps/s",
+            "sample": "every %dth instance (%d), full runs, one after another, the reference's "
+                      "kernels and launch shapes, its host-clock time" % (every, len(best)),
+            "seconds": t_us / 1e6, "kernels": "src/kernels.cu compiled to PTX, driven as "
+                                              "src/ising.cu drives them",
+            "best_cuts_mean": float(np.mean(best))}
+
+
 def run_reference(args, wl, rank):
     """--impl reference: the reference path has no CPU solver, so its CPU
     implementation here is the FP64 oracle port, every host thread."""
@@ -518,6 +544,18 @@ def main():
                 "kernel": kname, "bytes_per_launch": bytes_per_launch,
                 "launch_us": per_launch_s * 1e6, "launches": rp["kernel_launches"]}
 
+    ref_gpu = None
+    if rank == 0 and world == 1 and wl["kind"] == "maxcut":
+        import sbo
+        if sbo.ref_gpu_available():
+            og = sbo.Graph(inst.n, inst.rowptr, inst.col, inst.val, inst.wsum)
+            rr = sbo.ref_gpu_maxcut(og, A, wl["sb_steps"], wl["dt"], seed, uw=wl["update_window"],
+                                    fused=wl["fused"])
+            ref_gpu = {"value": nnz * A * rr["steps_run"] / (rr["time_us"] / 1e6),
+                       "unit": "nnz*agent*steps/s", "seconds": rr["time_us"] / 1e6,
+                       "best": rr["max"], "steps_run": rr["steps_run"],
+                       "kernels": "src/kernels.cu compiled to PTX, driven as src/ising.cu "
+                                  "drives them (FP64, its launch shapes, host-clock time)"}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         v, cores, s_cpu, dt = cpu_sample(wl, inst)
@@ -549,6 +587,7 @@ def main():
             "gpu_launches": launches,
             "roofline": roof,
             "cpu_baseline": cpu,
+            "reference_gpu": ref_gpu,
             "clocks": clocks,
             "other_precisions": others,
             "quality": qual,
@@ -722,6 +761,18 @@ def run_batch(args, wl, rank, world, local):
                 "kernel": "step kernel, one launch per SB step over all instances",
                 "bytes_per_launch": b_step, "launch_us": per_launch_s * 1e6,
                 "launches": rp[0]["kernel_launches"]}
+    # the same instances in FP16 state, and in FP32 from other seeds (the
+    # seed-to-seed spread of the best cut that any other trajectory shows)
+    spread = {}
+    for label, prec, off in (("f16", "f16", 0), ("f32_other_seeds", "f32", 100000)):
+        rs, _, _ = ctx.solve_batch(probs, agents, sbx.params(
+            dt=wl["dt"], steps=wl["sb_steps"], seed=seed + off, fused=wl["fused"],
+            precision=sbx.PRECISIONS[prec]))
+        b = np.array([r["max"] for r in rs])
+        g_ = (best_p - b) / np.abs(best_p)
+        spread[label] = {"within_0.1pct_of_fp32_plain": float(np.mean(g_ <= 1e-3)),
+                         "mean_rel_gap": float(np.mean(g_)), "max_rel_gap": float(np.max(g_))}
+    ref_gpu = reference_gpu_batch(wl, graphs, seed) if rank == 0 and world == 1 else None
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         v, cores, s_cpu, dt = cpu_batch_sample(wl, graphs, seconds=10.0)
@@ -750,7 +801,9 @@ def run_batch(args, wl, rank, world, local):
                         "within_0.1pct_of_fp32_plain": float(np.mean(rel <= 1e-3)),
                         "mean_rel_gap": float(np.mean(rel)), "max_rel_gap": float(np.max(rel)),
                         "energy_error_vs_f64": {"mean": float(np.mean(err64)),
-                                                "max": float(np.max(err64))}},
+                                                "max": float(np.max(err64))},
+                        "other_runs": spread},
+            "reference_gpu": ref_gpu,
             "time_to_target": ttt,
             "tile": {k: res[0][k] for k in ("kernel_used", "lane_agents", "row_lanes",
                                             "block_threads", "count_mode", "staging")},

@@ -94,7 +94,7 @@ extern "C" const char *ref_gpu_last_error(void) { return g_err.c_str(); }
 // ps of the cuts, SB steps run, windows run.  x, y (n * agents, row-major)
 // and cut (agents) are optional outputs.  run_windows > 0 stops after that
 // many windows (the first run_windows * 100 steps of the max_steps
-// schedule).
+// schedule); run_windows < 0 runs the pre-step Update_XY only.
 extern "C" int ref_gpu_maxcut(const char *ptx_path, int device, int64_t n64, int64_t nnz,
                               const int32_t *rowptr, const int32_t *col, const double *val, double wsum,
                               int agents, int max_steps, double dt, unsigned seed, int uw, int fused,
@@ -207,7 +207,7 @@ extern "C" int ref_gpu_maxcut(const char *ptx_path, int device, int64_t n64, int
         DRV(cuLaunchKernel(k.update_xy, gx, gy, 1, 32, 32, 1, 0, nullptr, a_xy, nullptr));
         DRV(cuCtxSynchronize());
         int64_t step = 0, windows = 0;
-        bool run = step < max_steps;
+        bool run = step < max_steps && run_windows >= 0;
         std::vector<unsigned char> bif((size_t)ncols);
         while (run) {
             DRV(cuGraphLaunch(exec, stream));

@@ -5,11 +5,15 @@ where the reference sources are (oracle/Makefile); oracle/_ref/libref_gpu.so
 drives those kernels as src/ising.cu does.  The tests skip where the PTX was
 not built.
 
-* One window (100 steps) of configuration 1 (ER n=800, 1024 agents, dt 0.1):
-  the reference's GPU state against the oracle's FP64 restatement of its
-  kernel.  They differ only where the reference's in-place update let a
-  thread read a neighbour already updated in the same launch, and by its
-  compiler's fused multiply-adds: most agents agree to 1e-9.
+* The set-up (configuration 1: ER n=800, 1024 agents, dt 0.1): the
+  reference's initial state after its pre-step Update_XY equals the oracle's
+  (to the rounding of its compiler's fused multiply-adds).
+* Its trajectories are not reproducible: the kernel updates X in place while
+  other threads gather it (src/kernels.cu:225-262), and early in a run, when
+  many x sit near zero, a gathered neighbour that has already moved this step
+  flips sign often.  After one window the reference's state is a different
+  trajectory from the Jacobi restatement's (and from another run's), so the
+  comparison is on whole runs:
 * Whole runs of configurations 1 and 2: the reference's best cut, and the
   engine's FP32-plain best cut from the same seed within 0.5% of it.
 """
@@ -30,18 +34,16 @@ def oracle_ref(oracle):
     return oracle
 
 
-def test_reference_gpu_first_window_matches_its_restatement(oracle_ref):
+def test_reference_gpu_setup_matches_the_oracle(oracle_ref):
     oracle = oracle_ref
     wl = bench.WORKLOADS["er800"]
     g = bench.build_instance(wl, oracle)
     A, steps, dt = wl["agents"], wl["sb_steps"], wl["dt"]
-    r = oracle.ref_gpu_maxcut(g, A, steps, dt, 1, run_windows=1, want_state=True)
-    assert r["steps_run"] == 100 and r["windows_run"] == 1
-    o = oracle.maxcut_solve(g, oracle.params(dt=dt, steps=steps, agents=A, seed=1, run_steps=100),
-                            want_state=True)
-    err = np.max(np.abs(r["x"].reshape(g.n, A) - o["x"].reshape(g.n, A)), axis=0)
-    assert np.median(err) < 1e-9
-    assert np.mean(err < 1e-6) > 0.9
+    r = oracle.ref_gpu_maxcut(g, A, steps, dt, 1, run_windows=-1, want_state=True)
+    assert r["steps_run"] == 0 and r["windows_run"] == 0
+    x, y = oracle.init_maxcut(g.n, A, 1)
+    oracle.update_xy(x, y, 0, steps, dt)
+    assert np.max(np.abs(r["x"] - x)) <= 1e-15 and np.max(np.abs(r["y"] - y)) <= 1e-15
 
 
 @pytest.mark.parametrize("name", ["er800", "torus"])
