@@ -46,8 +46,11 @@ enum { SBX_F32 = 0, SBX_BF16 = 1, SBX_F16 = 2, SBX_F64 = 3 };
 /* kernel family: chosen by shape (AUTO) or forced.  RESIDENT keeps a CTA's
  * agents in shared memory; RESIDENT_SPLIT (MaxCut, fused, 16-bit state) keeps
  * 8 agents per CTA split between registers and shared memory, for graphs too
- * large for the former. */
-enum { SBX_KERNEL_AUTO = 0, SBX_KERNEL_STREAM = 1, SBX_KERNEL_RESIDENT = 2, SBX_KERNEL_RESIDENT_SPLIT = 3 };
+ * large for the former.  TENSOR (TSP, 16-bit state, 3 <= N <= 32) is the
+ * resident TSP kernel with the distance product on the tensor cores
+ * (tcgen05): AUTO's choice for BF16 and FP16 TSP states that fit it. */
+enum { SBX_KERNEL_AUTO = 0, SBX_KERNEL_STREAM = 1, SBX_KERNEL_RESIDENT = 2, SBX_KERNEL_RESIDENT_SPLIT = 3,
+       SBX_KERNEL_TENSOR = 4 };
 /* TSP distance kinds, src/kernels.cu:404-442 */
 enum { SBX_DIST_EUC_2D = 0, SBX_DIST_GEO = 1, SBX_DIST_EUC_2D_FLOAT = 2 };
 /* sbx_params.flags */
@@ -56,7 +59,8 @@ enum { SBX_DIST_EUC_2D = 0, SBX_DIST_GEO = 1, SBX_DIST_EUC_2D_FLOAT = 2 };
 #define SBX_FLAG_PROFILE 4u     /* time every hot-kernel launch with events */
 #define SBX_FLAG_NO_TUNE 8u     /* streaming tile from the fixed heuristic, not timed */
 /* Test only: every bounded device wait of the solve (the co-resident window
- * barrier, the staged-row copy waits) gives up at its first check, as a wait
+ * barrier, the staged-row copy waits, the TSP tensor-core kernel's wait for
+ * its MMAs) gives up at its first check, as a wait
  * that never completes would after its limit.  The kernels flag the error,
  * let their copies in flight land and return; the solve returns SBX_ERR_CUDA
  * and the context stays usable for the next solve. */

@@ -866,6 +866,7 @@ int solve_tsp(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
     d.xi0 = 0.002;                                               // ising_tsp.cu:61
     d.c0 = d.dt * d.xi0;
     d.pdl = !(pr->flags & SBX_FLAG_NO_PDL);
+    d.giveup = (pr->flags & SBX_FLAG_TEST_GIVEUP) ? 1 : 0;
     const int32_t run = pr->run_steps > 0 ? std::min(pr->run_steps, pr->steps) : pr->steps;
     const int64_t nwin = d.period > 0 ? (run + d.period - 1) / d.period : 1;
     const int64_t total = d.period > 0 ? nwin * d.period : 0;
@@ -898,8 +899,14 @@ int solve_tsp(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
     CK(cudaMemcpyAsync(w.ab, ab.data(), ab.size() * 8, cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));
     if ((rc = init_state(ctx, d, pr->seed, true))) return rc;
-    int ka = 0;
-    if (pr->kernel != SBX_KERNEL_STREAM) ka = tsp_pick_ka(d, t, pr->agents_per_block);
+    // the tensor-core kernel for 16-bit states that fit it (AUTO or forced),
+    // else the CUDA-core resident kernel, else streaming
+    const bool tc = (pr->kernel == SBX_KERNEL_AUTO || pr->kernel == SBX_KERNEL_TENSOR) && tsp_tensor_fits(d, t) &&
+                    (pr->agents_per_block <= 0 || pr->agents_per_block == kTspTensorAgents);
+    if (pr->kernel == SBX_KERNEL_TENSOR && !tc)
+        return fail(ctx, SBX_ERR_UNSUPPORTED, "TSP tensor-core kernel: BF16/FP16 state and 3 <= N <= 32 only");
+    int ka = tc ? kTspTensorAgents : 0;
+    if (!tc && pr->kernel != SBX_KERNEL_STREAM) ka = tsp_pick_ka(d, t, pr->agents_per_block);
     if (pr->kernel == SBX_KERNEL_RESIDENT && !ka)
         return fail(ctx, SBX_ERR_UNSUPPORTED, "TSP resident kernel: N > 32, FP64 or tile too wide");
     if (!ka) {
@@ -909,7 +916,10 @@ int solve_tsp(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
     }
     int launches = 0, hot = 0;
     CK(cudaEventRecord(ctx->ev0, s));
-    if (ka) {
+    if (tc) {
+        CK(launch_tsp_tensor(d, t, w, s));
+        launches = hot = 1;
+    } else if (ka) {
         CK(launch_tsp_resident(d, t, w, ka, s));
         launches = hot = 1;
     } else {
@@ -972,7 +982,7 @@ int solve_tsp(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
     res->steps_run = ctl[CTL_STEP];
     res->windows_run = ctl[CTL_WINDOWS];
     for (uint8_t b : bif) res->bifurcated += b;
-    res->kernel_used = ka ? SBX_KERNEL_RESIDENT : SBX_KERNEL_STREAM;
+    res->kernel_used = tc ? SBX_KERNEL_TENSOR : ka ? SBX_KERNEL_RESIDENT : SBX_KERNEL_STREAM;
     res->agents_per_block = ka;
     res->kernel_launches = hot;
     // SBX_FLAG_PROFILE: the SB loop's kernels (the whole solve is one
@@ -1109,6 +1119,7 @@ void free_rb(DevRb &B)
 void free_bsm(DevBsm &M)
 {
     cudaFree(M.lcol);
+    cudaFree(M.rinfo);
     cudaFree(M.seg);
     cudaFree(M.cta_seg);
     cudaFree(M.ioff);
@@ -1138,9 +1149,21 @@ bool bsm_ok(const BatchClass &c, const SolveDims &d)
 int build_bsm(sbx_ctx *ctx, BatchClass &c, int W)
 {
     DevBsm &M = c.bsm;
-    const int64_t n = c.J.n, nnz = c.J.nnz;
+    const int64_t n = c.J.n;
     const size_t ni = c.probs.size();
-    std::vector<uint32_t> lcol((size_t)nnz);
+    // each row's entries padded to whole blocks of eight (the padding reads
+    // the instance's all-zero row); rinfo = first block << 7 | degree
+    std::vector<uint32_t> rinfo((size_t)n);
+    int64_t blocks = 0;
+    for (int64_t r = 0; r < n; r++) {
+        const int64_t deg = c.J.hrowptr[(size_t)r + 1] - c.J.hrowptr[(size_t)r];
+        if (deg > 127 || blocks >= ((int64_t)1 << 25))
+            return fail(ctx, SBX_ERR_UNSUPPORTED, "batch: shared-plane kernel row index out of range");
+        rinfo[(size_t)r] = (uint32_t)(blocks << 7) | (uint32_t)deg;
+        blocks += (deg + 7) / 8;
+    }
+    const int64_t nnz_p = blocks * 8;
+    std::vector<uint32_t> lcol((size_t)nnz_p);
     std::vector<int32_t> ioff(ni), in(ni);
     int64_t maxn = 0;
     for (size_t i = 0; i < ni; i++) {
@@ -1148,12 +1171,18 @@ int build_bsm(sbx_ctx *ctx, BatchClass &c, int W)
         ioff[i] = (int32_t)r0;
         in[i] = (int32_t)rn;
         maxn = std::max(maxn, rn);
-        for (int64_t e = c.J.hrowptr[(size_t)r0]; e < c.J.hrowptr[(size_t)(r0 + rn)]; e++) {
-            const int64_t lc = (int64_t)c.J.hcol[(size_t)e] - r0;
-            // the kernel reads the plane at this offset: it must be a row of
-            // the instance (a block-diagonal matrix guarantees it)
-            if (lc < 0 || lc >= rn) return fail(ctx, SBX_ERR_ARG, "batch: a column outside its instance");
-            lcol[(size_t)e] = (uint32_t)lc * (uint32_t)(4 * W) | (c.J.hval[(size_t)e] < 0 ? 0x80000000u : 0u);
+        const uint32_t zrow = (uint32_t)rn * (uint32_t)(4 * W);
+        for (int64_t r = r0; r < r0 + rn; r++) {
+            int64_t o = (int64_t)(rinfo[(size_t)r] >> 7) * 8;
+            const int64_t e1 = c.J.hrowptr[(size_t)r + 1];
+            for (int64_t e = c.J.hrowptr[(size_t)r]; e < e1; e++) {
+                const int64_t lc = (int64_t)c.J.hcol[(size_t)e] - r0;
+                // the kernel reads the plane at this offset: it must be a row
+                // of the instance (a block-diagonal matrix guarantees it)
+                if (lc < 0 || lc >= rn) return fail(ctx, SBX_ERR_ARG, "batch: a column outside its instance");
+                lcol[(size_t)o++] = (uint32_t)lc * (uint32_t)(4 * W) | (c.J.hval[(size_t)e] < 0 ? 0x80000000u : 0u);
+            }
+            while (o & 7) lcol[(size_t)o++] = zrow;
         }
     }
     const int grid = std::max(1, dev_attr(cudaDevAttrMultiProcessorCount));
@@ -1185,12 +1214,14 @@ int build_bsm(sbx_ctx *ctx, BatchClass &c, int W)
     }
     cta[(size_t)grid] = (int32_t)(seg.size() / 3);
     free_bsm(M);
-    CK(cudaMalloc(&M.lcol, sizeof(uint32_t) * std::max<int64_t>(nnz, 1)));
+    CK(cudaMalloc(&M.lcol, sizeof(uint32_t) * std::max<int64_t>(nnz_p, 8)));
+    CK(cudaMalloc(&M.rinfo, sizeof(uint32_t) * std::max<int64_t>(n, 1)));
     CK(cudaMalloc(&M.seg, sizeof(int32_t) * std::max<size_t>(seg.size(), 3)));
     CK(cudaMalloc(&M.cta_seg, sizeof(int32_t) * cta.size()));
     CK(cudaMalloc(&M.ioff, sizeof(int32_t) * ni));
     CK(cudaMalloc(&M.in, sizeof(int32_t) * ni));
-    if (nnz) CK(cudaMemcpy(M.lcol, lcol.data(), sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice));
+    if (nnz_p) CK(cudaMemcpy(M.lcol, lcol.data(), sizeof(uint32_t) * nnz_p, cudaMemcpyHostToDevice));
+    if (n) CK(cudaMemcpy(M.rinfo, rinfo.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
     if (!seg.empty()) CK(cudaMemcpy(M.seg, seg.data(), sizeof(int32_t) * seg.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(M.cta_seg, cta.data(), sizeof(int32_t) * cta.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(M.ioff, ioff.data(), sizeof(int32_t) * ni, cudaMemcpyHostToDevice));
@@ -1961,6 +1992,9 @@ int sbx_solve(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_resu
     ctx->have = false;
     ctx->batch_last = -1;   // the work buffers are about to be reused
     if (p->tsp && pr->target > 0) return fail(ctx, SBX_ERR_UNSUPPORTED, "target: MaxCut only");
+    if (pr->kernel < 0 || pr->kernel > SBX_KERNEL_TENSOR) return fail(ctx, SBX_ERR_ARG, "bad params: kernel");
+    if (!p->tsp && pr->kernel == SBX_KERNEL_TENSOR)
+        return fail(ctx, SBX_ERR_UNSUPPORTED, "the tensor-core kernel is the TSP distance product's");
     return p->tsp ? solve_tsp(ctx, p, pr, res, agent_values) : solve_maxcut(ctx, p, pr, res, agent_values);
 }
 

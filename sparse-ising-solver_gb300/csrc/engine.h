@@ -159,7 +159,9 @@ struct SolveDims {
 // memory (k_batch_smem.cu): the rows cut into one contiguous run per CTA,
 // each run into segments at instance boundaries.
 struct DevBsm {
-    uint32_t *lcol = nullptr;     // per entry: local column * 4W, weight sign in bit 31
+    uint32_t *lcol = nullptr;     // per entry: local column * 4W, weight sign in bit 31; rows
+                                  // padded to blocks of eight with the all-zero row's offset
+    uint32_t *rinfo = nullptr;    // per row: first block of eight entries << 7 | degree
     int32_t *seg = nullptr;       // per segment: instance, first row, end row (global rows)
     int32_t *cta_seg = nullptr;   // per CTA: first segment; grid + 1 entries
     int32_t *ioff = nullptr;      // per instance: first row
@@ -266,6 +268,11 @@ cudaError_t launch_tsp_resident(const SolveDims &d, const DevTsp &t, Work &w, in
                                 cudaStream_t s);
 cudaError_t launch_tsp_stream(const SolveDims &d, const DevTsp &t, Work &w, cudaStream_t s,
                               int *launches);
+// Resident TSP kernel with the distance product on the tensor cores
+// (k_tsp_tc.cu): 16-bit state, 3 <= N <= 32, 8 agents per CTA.
+bool tsp_tensor_fits(const SolveDims &d, const DevTsp &t);
+constexpr int kTspTensorAgents = 8;
+cudaError_t launch_tsp_tensor(const SolveDims &d, const DevTsp &t, Work &w, cudaStream_t s);
 // TSP setup on the device from city coordinates (device xc, yc): packed
 // distances (src/kernels.cu:404-442), the tables t.D / t.Dd, the largest
 // distance *mx, per-city sums (src/tsp_gpu.cu:51-68) and the linear field

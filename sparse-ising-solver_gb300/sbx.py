@@ -17,7 +17,7 @@ OK = 0
 ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_IO, ERR_FORMAT, ERR_UNSUPPORTED, ERR_NODEVICE, ERR_STATE = \
     -1, -2, -3, -4, -5, -6, -7, -8
 F32, BF16, F16, F64 = 0, 1, 2, 3
-KERNEL_AUTO, KERNEL_STREAM, KERNEL_RESIDENT, KERNEL_RESIDENT_SPLIT = 0, 1, 2, 3
+KERNEL_AUTO, KERNEL_STREAM, KERNEL_RESIDENT, KERNEL_RESIDENT_SPLIT, KERNEL_TENSOR = 0, 1, 2, 3, 4
 DIST_EUC_2D, DIST_GEO, DIST_EUC_2D_FLOAT = 0, 1, 2
 FLAG_NO_PDL, FLAG_NO_GRAPH, FLAG_PROFILE, FLAG_NO_TUNE, FLAG_TEST_GIVEUP = 1, 2, 4, 8, 16
 PRECISIONS = {"f32": F32, "bf16": BF16, "f16": F16, "f64": F64}

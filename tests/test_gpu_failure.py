@@ -6,9 +6,10 @@ A test-only flag (SBX_FLAG_TEST_GIVEUP) makes every bounded wait of a solve
 give up at its first check, the path a wait that never completes takes after
 its limit: the co-resident window barrier of the register + shared-memory
 resident kernel (its target raised past what the CTAs can reach, a short
-limit), and the staged-row copy waits of the streaming step kernel (the
-copies still land before the kernel returns).  Nothing faults, traps or
-hangs.
+limit), the staged-row copy waits of the streaming step kernel (the copies
+still land before the kernel returns) and the MMA-completion wait of the TSP
+tensor-core kernel (the MMAs finish and TMEM is freed before it returns).
+Nothing faults, traps or hangs.
 """
 import numpy as np
 import pytest
@@ -72,3 +73,22 @@ def test_staged_row_waits_give_up_single_and_batched(ctx, oracle):
     x, y, s = ctx.state(g.n, 64)
     assert np.array_equal(x, o["x"]) and np.array_equal(y, o["y"])
     assert np.array_equal(cut, o["cut"])
+
+
+def test_tensor_core_wait_gives_up_and_the_context_recovers(ctx):
+    # The TSP tensor-core kernel waits (bounded) for its MMAs on an mbarrier;
+    # giving up flags the error, drains the MMAs in flight, frees TMEM and
+    # returns.  The next solve is bit-identical to a solve on a fresh start.
+    xc, yc = sbx.gen_cities(16, 1000.0, seed=2)
+    packed = sbx.tsp_distances(xc, yc, sbx.DIST_EUC_2D_FLOAT)
+    mx = float(packed.max())
+    prob = ctx.tsp_problem(packed, 16, A=1.0, B=1.5 * mx, C_=1.5 * mx)
+    base = dict(dt=0.1, steps=400, agents=64, seed=4, precision=sbx.BF16, kernel=sbx.KERNEL_TENSOR)
+    r0, l0 = ctx.solve(prob, sbx.params(**base))
+    x0, y0, _ = ctx.state(256, 64)
+    _expect_wait_failure(lambda: ctx.solve(prob, sbx.params(flags=sbx.FLAG_TEST_GIVEUP, **base)))
+    r1, l1 = ctx.solve(prob, sbx.params(**base))
+    x1, y1, _ = ctx.state(256, 64)
+    assert r1["kernel_used"] == sbx.KERNEL_TENSOR and r1["steps_run"] == 400
+    assert np.array_equal(x0, x1) and np.array_equal(y0, y1)
+    assert np.array_equal(np.nan_to_num(l0), np.nan_to_num(l1))
