@@ -19,7 +19,17 @@
 // rounding to the storage type per store, so the state is bit-identical.
 //
 // Columns are stored as byte offsets into the instance's plane
-// (local column * 4W), the weight's sign in bit 31.
+// (local column * 4W), the weight's sign in bit 31, each row's list padded
+// to whole blocks of eight with the all-zero row and 32-byte aligned, so a
+// block of neighbours is two 16-byte loads; one word per row packs its first
+// block and its degree.
+//
+// At 64 agents (two words per row) the two lanes of a row interleave their
+// 8-agent chunks of x and y: in each of the four vector loads they read the
+// two halves of one 32-byte sector, which halves the sectors the state moves
+// through L1.  A lane counts its own 32-agent word, the pair swaps the counts
+// of the chunks the other updates, and swaps the new sign bytes back into
+// words.
 #include "k_step.cuh"
 
 namespace sbx {
@@ -27,7 +37,8 @@ namespace sbx {
 namespace {
 
 struct BsmP {
-    const uint32_t *__restrict__ lcol;    // per entry: local column * 4W | sign << 31
+    const uint32_t *__restrict__ lcol;    // per entry: local column * 4W | sign << 31, padded rows
+    const uint32_t *__restrict__ rinfo;   // per row: first block of eight entries << 7 | degree
     const int32_t *__restrict__ seg;      // per segment: instance, first row, end row (global)
     const int32_t *__restrict__ cta_seg;  // per CTA: first segment (grid + 1 entries)
     const int32_t *__restrict__ ioff;     // per instance: first row
@@ -68,6 +79,7 @@ __global__ void __launch_bounds__(NT, 1) k_bsm(const StepP P, const BsmP B, cons
     const bool cs = P.stream_state != 0;
     const int q = lane % W;                  // this lane's word of its row
     const uint32_t qbase = (uint32_t)__cvta_generic_to_shared(s_plane) + 4u * (uint32_t)q;
+    constexpr bool IL = W == 2;              // interleaved chunks (see above)
     int loaded = -1;
     for (int s = __ldg(&B.cta_seg[blockIdx.x]); s < __ldg(&B.cta_seg[blockIdx.x + 1]); s++) {
         const int inst = __ldg(&B.seg[3 * s]);
@@ -75,7 +87,7 @@ __global__ void __launch_bounds__(NT, 1) k_bsm(const StepP P, const BsmP B, cons
         const int ni = __ldg(&B.in[inst]);
         if (inst != loaded) {
             // the instance's plane (written by the previous step) and the
-            // all-zero row that neighbours past a row's end read
+            // all-zero row that padded neighbours read
             __syncthreads();
             const uint32_t *src = Scur + (int64_t)__ldg(&B.ioff[inst]) * W;
             for (int i = tid; i < ni * W; i += NT) s_plane[i] = __ldcg(src + i);
@@ -83,22 +95,26 @@ __global__ void __launch_bounds__(NT, 1) k_bsm(const StepP P, const BsmP B, cons
             __syncthreads();
             loaded = inst;
         }
-        const uint32_t zoff = (uint32_t)ni * (uint32_t)(4 * W);
+        // dt * xi0 is one value per instance
+        const float c0 = __ldg(&P.c0r32[r0]);
         const int ngroups = (r1 - r0 + RPW - 1) / RPW;
         for (int g = wid; g < ngroups; g += NW) {
             const int rr = r0 + g * RPW + lane / W;
             const bool live = rr < r1;
             const int r = live ? rr : r1 - 1;    // lanes past the segment repeat its last row
-            const int64_t base = (int64_t)r * P.Ap + 32 * q;
+            const int64_t rbase = (int64_t)r * P.Ap;
+            // the lane's four 8-agent chunks: its word's (32 q + 8 k), or
+            // interleaved with its partner's (8 (2 k + q))
+            auto chunk = [&](int k) { return IL ? 8 * (2 * k + q) : 32 * q + 8 * k; };
             // x of the lane's 32 agents in flight during the count (y after
             // it: both at once would spill the count's registers)
             Raw<16> xr[4], yr[4];
 #pragma unroll
-            for (int k = 0; k < 4; k++) xr[k] = vload_s<T, 8>(xp + base + 8 * k, cs);
+            for (int k = 0; k < 4; k++) xr[k] = vload_s<T, 8>(xp + rbase + chunk(k), cs);
             uint32_t wp_old = 0;
             if (WIN) wp_old = P.Wp[(int64_t)r * W + q];
-            const int32_t e0 = __ldg(&P.rowptr[r]);
-            const int32_t deg = live ? __ldg(&P.rowptr[r + 1]) - e0 : 0;
+            const uint32_t ri = __ldg(&B.rinfo[r]);
+            const int32_t deg = live ? (int32_t)(ri & 127u) : 0;
             const int32_t dmax = __reduce_max_sync(FULL, deg);
             // seven bit planes of the count of agents whose neighbour term is
             // -1 (bit a of p[k] = bit k of agent a's count), Harley-Seal
@@ -106,15 +122,21 @@ __global__ void __launch_bounds__(NT, 1) k_bsm(const StepP P, const BsmP B, cons
             uint32_t p[7];
 #pragma unroll
             for (int k = 0; k < 7; k++) p[k] = 0;
-            const uint32_t *cp = B.lcol + e0;
+            const uint4 *cp = (const uint4 *)(B.lcol + (size_t)(ri >> 7) * 8);
+            const uint32_t zoff = (uint32_t)ni * (uint32_t)(4 * W);
             for (int32_t kb = 0; kb < dmax; kb += 8) {
+                uint4 ca = make_uint4(zoff, zoff, zoff, zoff), cb = ca;
+                if (kb < deg) {
+                    ca = __ldg(cp + kb / 4);
+                    cb = __ldg(cp + kb / 4 + 1);
+                }
+                const uint32_t cw[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
                 uint32_t w[8];
 #pragma unroll
                 for (int j = 0; j < 8; j++) {
-                    const uint32_t cw = kb + j < deg ? __ldg(cp + kb + j) : zoff;
                     uint32_t word;
-                    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(word) : "r"(qbase + (cw & 0x7fffffffu)));
-                    w[j] = P.allpos ? word : word ^ (uint32_t)((int32_t)cw >> 31);
+                    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(word) : "r"(qbase + (cw[j] & 0x7fffffffu)));
+                    w[j] = P.allpos ? word : word ^ (uint32_t)((int32_t)cw[j] >> 31);
                 }
                 const uint32_t a1 = fa(p[0], w[0], w[1]);
                 const uint32_t b1 = fa(p[0], w[2], w[3]);
@@ -131,9 +153,9 @@ __global__ void __launch_bounds__(NT, 1) k_bsm(const StepP P, const BsmP B, cons
                 }
             }
             // the planes as byte counters: byte v of cnt[2k + v / 4] = 2 * count
-            // of agent 8k + v.  Byte k of each plane goes to one byte of a
-            // 64-bit value shifted up a byte (which doubles the counts), then
-            // an 8x8 bit transpose (rows = bytes).
+            // of agent 8k + v of the word.  Byte k of each plane goes to one
+            // byte of a 64-bit value shifted up a byte (which doubles the
+            // counts), then an 8x8 bit transpose (rows = bytes).
             uint32_t cnt[8];
 #pragma unroll
             for (int k = 0; k < 4; k++) {
@@ -155,18 +177,40 @@ __global__ void __launch_bounds__(NT, 1) k_bsm(const StepP P, const BsmP B, cons
                 cnt[2 * k] = lo;
                 cnt[2 * k + 1] = hi;
             }
-            const float c0 = __ldg(&P.c0r32[r]);
+            if (IL) {
+                // lane q updates the chunks c = q, q + 2 of both words: its
+                // own word's, and the partner's sent across (the partner
+                // sends its chunks 1 - q, 3 - q)
+#pragma unroll
+                for (int j = 0; j < 2; j++) {
+                    const uint32_t s0 = q ? cnt[4 * j] : cnt[4 * j + 2];
+                    const uint32_t s1 = q ? cnt[4 * j + 1] : cnt[4 * j + 3];
+                    const uint32_t r0v = __shfl_xor_sync(FULL, s0, 1);
+                    const uint32_t r1v = __shfl_xor_sync(FULL, s1, 1);
+                    // chunk k = j (word 0) and k = 2 + j (word 1)
+                    const uint32_t o0 = q ? cnt[4 * j + 2] : cnt[4 * j];
+                    const uint32_t o1 = q ? cnt[4 * j + 3] : cnt[4 * j + 1];
+                    // word 0 holds lane 0's own counts, word 1 lane 1's
+                    cnt[4 * j] = q ? r0v : o0;        // k = j (word 0)
+                    cnt[4 * j + 1] = q ? r1v : o1;
+                    cnt[4 * j + 2] = q ? o0 : r0v;    // k = 2 + j (word 1)
+                    cnt[4 * j + 3] = q ? o1 : r1v;
+                }
+            }
             // PRMT builds the float 2^23 + 2 count; minus 2^23 + degree it is
             // the force 2 count - degree, exactly
             const float bias = 8388608.0f + (float)deg;
             uint32_t b = 0;
 #pragma unroll
             for (int k = 0; k < 4; k++) {
-                yr[k] = vload_s<T, 8>(yp + base + 8 * k, cs);
+                yr[k] = vload_s<T, 8>(yp + rbase + chunk(k), cs);
+                // the counts of chunk k: cnt[2k], cnt[2k + 1] (word order), or
+                // in the interleaved order cnt[4 (k % 2) + 2 (k / 2)] ...
+                const int ci = IL ? 4 * (k % 2) + 2 * (k / 2) : 2 * k;
                 float tv[8], x[8], y[8];
 #pragma unroll
                 for (int v = 0; v < 8; v++)
-                    tv[v] = __uint_as_float(__byte_perm(cnt[2 * k + v / 4], 0x4b000000u, 0x7440u + (v & 3))) - bias;
+                    tv[v] = __uint_as_float(__byte_perm(cnt[ci + v / 4], 0x4b000000u, 0x7440u + (v & 3))) - bias;
                 to_vals<T, 8>(xr[k], x);
                 to_vals<T, 8>(yr[k], y);
                 sb_update<KIND, WIN, 8>(x, y, tv, c0, c, cn);
@@ -175,11 +219,17 @@ __global__ void __launch_bounds__(NT, 1) k_bsm(const StepP P, const BsmP B, cons
                 xr[k] = from_vals<T, 8>(x);
                 yr[k] = from_vals<T, 8>(y);
             }
+            if (IL) {
+                // byte k of b: the signs of chunk 2 k + q; word q is the
+                // chunks 4 q .. 4 q + 3, alternately the two lanes' bytes
+                const uint32_t pb = __shfl_xor_sync(FULL, b, 1);
+                b = q ? __byte_perm(b, pb, 0x3726) : __byte_perm(b, pb, 0x5140);
+            }
             if (live) {
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
-                    vstore_s(xp + base + 8 * k, xr[k].u, cs);
-                    vstore_s(yp + base + 8 * k, yr[k].u, cs);
+                    vstore_s(xp + rbase + chunk(k), xr[k].u, cs);
+                    vstore_s(yp + rbase + chunk(k), yr[k].u, cs);
                 }
                 const int64_t wi = (int64_t)r * W + q;
                 if (KIND == K_FUSED || !WIN) Snext[wi] = b;
@@ -251,6 +301,7 @@ cudaError_t launch_batch_smem(const SolveDims &d, const DevBsm &M, const StepP &
 {
     BsmP B;
     B.lcol = M.lcol;
+    B.rinfo = M.rinfo;
     B.seg = M.seg;
     B.cta_seg = M.cta_seg;
     B.ioff = M.ioff;
