@@ -22,6 +22,7 @@
 #include "csr.cuh"
 #include "kernels.cuh"
 
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -394,12 +395,39 @@ int dump_tsp(const char *path, const char *out)
     return 0;
 }
 
+/* Loader timing: the reference's CSR (src/csr.cpp) or TSP_CPU
+ * (src/tsp_cpu.cpp) constructor on one file, `reps` times, one thread as the
+ * reference runs it; prints the fastest wall time in seconds and the sizes. */
+int time_loader(const char *kind, const char *path, int reps)
+{
+    double best = 1e300;
+    long long a = 0, b = 0;
+    for (int i = 0; i < reps; i++) {
+        const auto t0 = std::chrono::steady_clock::now();
+        if (std::string(kind) == "mtx-time") {
+            CSR csr(path);
+            a = csr.size;
+            b = csr.nonzeros;
+        } else {
+            TSP_CPU tsp(path);
+            a = tsp.ncities;
+        }
+        const double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        best = s < best ? s : best;
+    }
+    printf("%.9f %lld %lld\n", best, a, b);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv)
 {
+    if (argc == 4 && (std::string(argv[1]) == "mtx-time" || std::string(argv[1]) == "tsplib-time"))
+        return time_loader(argv[1], argv[2], atoi(argv[3]));
     if (argc != 4) {
-        fprintf(stderr, "usage: ref_kernels maxcut|tsp|mtx|tsplib <in> <out>\n");
+        fprintf(stderr, "usage: ref_kernels maxcut|tsp|mtx|tsplib <in> <out>\n"
+                        "       ref_kernels mtx-time|tsplib-time <in> <repetitions>\n");
         return 2;
     }
     std::string mode = argv[1];
