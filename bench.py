@@ -886,6 +886,7 @@ def run_batch(args, wl, rank, world, local):
     # that reaches the last targets counts up to its slowest instance.
     t_restart = float(np.max(tb)) if reached.all() else None
     rounds, missed = 0, np.nonzero(~reached)[0]
+    left = [int(len(missed))]
     if not reached.all():
         t_restart = t_first = float(rt[0]["time_us"]) if rt[0]["time_us"] > 0 else None
         t_restart = t_first
@@ -899,6 +900,7 @@ def run_batch(args, wl, rank, world, local):
             ok = tr_ > 0
             t_restart += float(tr_.max()) if ok.all() else float(t_sub)
             missed = missed[~ok]
+            left.append(int(len(missed)))
         if len(missed):
             t_restart = None
     ttt = {"rule": "per instance: FP32-plain best cut less 0.1%",
@@ -909,6 +911,7 @@ def run_batch(args, wl, rank, world, local):
            "speedup": float(tp.sum() / tb.max()) if reached.all() else None,
            "missed": [int(i) for i in np.nonzero(~reached)[0]],
            "with_restarts": {"rounds": rounds, "all_reached": t_restart is not None,
+                             "missed_after_each_round": left,
                              "batched_us": t_restart,
                              "speedup": float(tp.sum() / t_restart) if t_restart else None}}
     peaks, peak_kind = load_peaks()

@@ -272,7 +272,10 @@ cudaError_t launch_tsp_stream(const SolveDims &d, const DevTsp &t, Work &w, cuda
 // (k_tsp_tc.cu): 16-bit state, 3 <= N <= 32, 8 agents per CTA.
 bool tsp_tensor_fits(const SolveDims &d, const DevTsp &t);
 constexpr int kTspTensorAgents = 8;
-cudaError_t launch_tsp_tensor(const SolveDims &d, const DevTsp &t, Work &w, cudaStream_t s);
+// threads_per_row: 1, 2 or 4 threads share a (position, agent) row's
+// cities; 0 picks the default.
+int tsp_tensor_threads_per_row(int requested);
+cudaError_t launch_tsp_tensor(const SolveDims &d, const DevTsp &t, Work &w, int threads_per_row, cudaStream_t s);
 // TSP setup on the device from city coordinates (device xc, yc): packed
 // distances (src/kernels.cu:404-442), the tables t.D / t.Dd, the largest
 // distance *mx, per-city sums (src/tsp_gpu.cu:51-68) and the linear field

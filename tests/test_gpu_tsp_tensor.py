@@ -127,3 +127,18 @@ def test_auto_picks_tensor_for_16_bit_tsp_only(ctx):
     with pytest.raises(sbx.SbxError) as e:
         ctx.solve(g, sbx.params(precision=sbx.BF16, kernel=sbx.KERNEL_TENSOR, **kw))
     assert e.value.rc == sbx.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("threads", [1, 2, 4])
+@pytest.mark.parametrize("N", [13, 30])
+def test_threads_per_row_agree(ctx, N, threads):
+    # 1, 2 or 4 threads share a row's cities (row_lanes): the same arithmetic
+    # in the same order, so the states are bit-identical
+    prob, _ = _problem(ctx, N, 1000.0, seed=N + 1)
+    A = 48
+    kw = dict(dt=0.1, steps=600, run_steps=300, seed=3)
+    r, xt, yt, lt = _run(ctx, prob, N, A, sbx.BF16, sbx.KERNEL_TENSOR, row_lanes=threads, **kw)
+    assert r["row_lanes"] == threads
+    r1, x1, y1, l1 = _run(ctx, prob, N, A, sbx.BF16, sbx.KERNEL_TENSOR, row_lanes=1, **kw)
+    assert np.array_equal(xt, x1) and np.array_equal(yt, y1)
+    assert np.array_equal(np.nan_to_num(lt), np.nan_to_num(l1)) and r["valid"] == r1["valid"]
