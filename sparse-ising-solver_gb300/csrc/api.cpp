@@ -1130,7 +1130,8 @@ void free_bsm(DevBsm &M)
 
 // Can the class run the shared-memory-plane step kernel: 16-bit state, +-1
 // weights, at most 127 neighbours per row (seven count planes), 32, 64 or 128
-// padded agents, and the largest instance's plane fits in shared memory.
+// padded agents, instances of at most 32,767 rows (15-bit local columns), and
+// the largest instance's plane fits in shared memory.
 bool bsm_ok(const BatchClass &c, const SolveDims &d)
 {
     if (d.prec != P_BF16 && d.prec != P_F16) return false;
@@ -1138,6 +1139,7 @@ bool bsm_ok(const BatchClass &c, const SolveDims &d)
     if (d.W != 1 && d.W != 2 && d.W != 4) return false;
     int64_t maxn = 0;
     for (const sbx_problem *q : c.probs) maxn = std::max<int64_t>(maxn, q->J.n);
+    if (maxn > 32767) return false;
     const int optin = dev_attr(cudaDevAttrMaxSharedMemoryPerBlockOptin);
     return (int64_t)bsm_smem_bytes(maxn, d.W) + 1024 <= (int64_t)optin;
 }
@@ -1164,7 +1166,7 @@ int build_bsm(sbx_ctx *ctx, BatchClass &c, int W)
         blocks += (deg + 7) / 8;
     }
     const int64_t nnz_p = blocks * 8;
-    std::vector<uint32_t> lcol((size_t)nnz_p);
+    std::vector<uint16_t> lcol((size_t)nnz_p);
     std::vector<int32_t> ioff(ni), in(ni);
     int64_t maxn = 0;
     for (size_t i = 0; i < ni; i++) {
@@ -1172,7 +1174,8 @@ int build_bsm(sbx_ctx *ctx, BatchClass &c, int W)
         ioff[i] = (int32_t)r0;
         in[i] = (int32_t)rn;
         maxn = std::max(maxn, rn);
-        const uint32_t zrow = (uint32_t)rn * (uint32_t)(4 * W);
+        if (rn > 32767) return fail(ctx, SBX_ERR_UNSUPPORTED, "batch: shared-plane kernel instance too large");
+        const uint16_t zrow = (uint16_t)rn;
         for (int64_t r = r0; r < r0 + rn; r++) {
             int64_t o = (int64_t)(rinfo[(size_t)r] >> 7) * 8;
             const int64_t e1 = c.J.hrowptr[(size_t)r + 1];
@@ -1181,7 +1184,7 @@ int build_bsm(sbx_ctx *ctx, BatchClass &c, int W)
                 // the kernel reads the plane at this offset: it must be a row
                 // of the instance (a block-diagonal matrix guarantees it)
                 if (lc < 0 || lc >= rn) return fail(ctx, SBX_ERR_ARG, "batch: a column outside its instance");
-                lcol[(size_t)o++] = (uint32_t)lc * (uint32_t)(4 * W) | (c.J.hval[(size_t)e] < 0 ? 0x80000000u : 0u);
+                lcol[(size_t)o++] = (uint16_t)((uint32_t)lc | (c.J.hval[(size_t)e] < 0 ? 0x8000u : 0u));
             }
             while (o & 7) lcol[(size_t)o++] = zrow;
         }
@@ -1215,13 +1218,13 @@ int build_bsm(sbx_ctx *ctx, BatchClass &c, int W)
     }
     cta[(size_t)grid] = (int32_t)(seg.size() / 3);
     free_bsm(M);
-    CK(cudaMalloc(&M.lcol, sizeof(uint32_t) * std::max<int64_t>(nnz_p, 8)));
+    CK(cudaMalloc(&M.lcol, sizeof(uint16_t) * std::max<int64_t>(nnz_p, 8)));
     CK(cudaMalloc(&M.rinfo, sizeof(uint32_t) * std::max<int64_t>(n, 1)));
     CK(cudaMalloc(&M.seg, sizeof(int32_t) * std::max<size_t>(seg.size(), 3)));
     CK(cudaMalloc(&M.cta_seg, sizeof(int32_t) * cta.size()));
     CK(cudaMalloc(&M.ioff, sizeof(int32_t) * ni));
     CK(cudaMalloc(&M.in, sizeof(int32_t) * ni));
-    if (nnz_p) CK(cudaMemcpy(M.lcol, lcol.data(), sizeof(uint32_t) * nnz_p, cudaMemcpyHostToDevice));
+    if (nnz_p) CK(cudaMemcpy(M.lcol, lcol.data(), sizeof(uint16_t) * nnz_p, cudaMemcpyHostToDevice));
     if (n) CK(cudaMemcpy(M.rinfo, rinfo.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
     if (!seg.empty()) CK(cudaMemcpy(M.seg, seg.data(), sizeof(int32_t) * seg.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(M.cta_seg, cta.data(), sizeof(int32_t) * cta.size(), cudaMemcpyHostToDevice));

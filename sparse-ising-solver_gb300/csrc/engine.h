@@ -159,8 +159,8 @@ struct SolveDims {
 // memory (k_batch_smem.cu): the rows cut into one contiguous run per CTA,
 // each run into segments at instance boundaries.
 struct DevBsm {
-    uint32_t *lcol = nullptr;     // per entry: local column * 4W, weight sign in bit 31; rows
-                                  // padded to blocks of eight with the all-zero row's offset
+    uint16_t *lcol = nullptr;     // per entry: local column | weight sign << 15; rows padded
+                                  // to blocks of eight with the all-zero row (local row n_i)
     uint32_t *rinfo = nullptr;    // per row: first block of eight entries << 7 | degree
     int32_t *seg = nullptr;       // per segment: instance, first row, end row (global rows)
     int32_t *cta_seg = nullptr;   // per CTA: first segment; grid + 1 entries

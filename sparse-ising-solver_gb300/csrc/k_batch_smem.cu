@@ -18,11 +18,10 @@
 // the force 2 count - degree is exact, the update is sb_update in FP32, one
 // rounding to the storage type per store, so the state is bit-identical.
 //
-// Columns are stored as byte offsets into the instance's plane
-// (local column * 4W), the weight's sign in bit 31, each row's list padded
-// to whole blocks of eight with the all-zero row and 32-byte aligned, so a
-// block of neighbours is two 16-byte loads; one word per row packs its first
-// block and its degree.
+// Columns are 16-bit local rows (instances of at most 32,767 rows) with the
+// weight's sign in bit 15, each row's list padded to whole blocks of eight
+// with the all-zero row and 16-byte aligned, so a block of neighbours is one
+// 16-byte load; one word per row packs its first block and its degree.
 //
 // At 64 agents (two words per row) the two lanes of a row interleave their
 // 8-agent chunks of x and y: in each of the four vector loads they read the
@@ -37,7 +36,7 @@ namespace sbx {
 namespace {
 
 struct BsmP {
-    const uint32_t *__restrict__ lcol;    // per entry: local column * 4W | sign << 31, padded rows
+    const uint4 *__restrict__ lcol;       // blocks of eight 16-bit entries: local column | sign << 15
     const uint32_t *__restrict__ rinfo;   // per row: first block of eight entries << 7 | degree
     const int32_t *__restrict__ seg;      // per segment: instance, first row, end row (global)
     const int32_t *__restrict__ cta_seg;  // per CTA: first segment (grid + 1 entries)
@@ -122,21 +121,27 @@ __global__ void __launch_bounds__(NT, 1) k_bsm(const StepP P, const BsmP B, cons
             uint32_t p[7];
 #pragma unroll
             for (int k = 0; k < 7; k++) p[k] = 0;
-            const uint4 *cp = (const uint4 *)(B.lcol + (size_t)(ri >> 7) * 8);
-            const uint32_t zoff = (uint32_t)ni * (uint32_t)(4 * W);
+            const uint4 *cp = B.lcol + (ri >> 7);
+            const uint32_t zpair = (uint32_t)ni * 0x10001u;   // two entries of the zero row
             for (int32_t kb = 0; kb < dmax; kb += 8) {
-                uint4 ca = make_uint4(zoff, zoff, zoff, zoff), cb = ca;
-                if (kb < deg) {
-                    ca = __ldg(cp + kb / 4);
-                    cb = __ldg(cp + kb / 4 + 1);
-                }
-                const uint32_t cw[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
+                uint4 cv = make_uint4(zpair, zpair, zpair, zpair);
+                if (kb < deg) cv = __ldg(cp + kb / 8);
+                const uint32_t pv[4] = {cv.x, cv.y, cv.z, cv.w};
                 uint32_t w[8];
 #pragma unroll
                 for (int j = 0; j < 8; j++) {
+                    const uint32_t v = pv[j / 2];
+                    const uint32_t col = (j & 1) ? (v >> 16) & 0x7fffu : v & 0x7fffu;
                     uint32_t word;
-                    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(word) : "r"(qbase + (cw[j] & 0x7fffffffu)));
-                    w[j] = P.allpos ? word : word ^ (uint32_t)((int32_t)cw[j] >> 31);
+                    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(word) : "r"(qbase + col * (uint32_t)(4 * W)));
+                    if (!P.allpos) {
+                        // the sign bit (15 or 31) replicated over the word
+                        uint32_t neg;
+                        if (j & 1) asm("prmt.b32 %0, %1, 0, 0xbbbb;" : "=r"(neg) : "r"(v));
+                        else asm("prmt.b32 %0, %1, 0, 0x9999;" : "=r"(neg) : "r"(v));
+                        word ^= neg;
+                    }
+                    w[j] = word;
                 }
                 const uint32_t a1 = fa(p[0], w[0], w[1]);
                 const uint32_t b1 = fa(p[0], w[2], w[3]);
@@ -300,7 +305,7 @@ cudaError_t launch_batch_smem(const SolveDims &d, const DevBsm &M, const StepP &
                               int offset, cudaStream_t s)
 {
     BsmP B;
-    B.lcol = M.lcol;
+    B.lcol = (const uint4 *)M.lcol;
     B.rinfo = M.rinfo;
     B.seg = M.seg;
     B.cta_seg = M.cta_seg;

@@ -338,6 +338,9 @@ __global__ void __launch_bounds__(128 * 2 * H, 1) k_tsp_tc(const TcP P)
                     rsum[m] = rs;
                 }
             }
+            // the products are in TMEM once every thread's wait ends; the
+            // barrier also publishes colsum and rsum and ends this step's
+            // reads of X, so X may be rewritten after it
             const bool ok = mbar_wait_n(bar, phase, P.giveup ? 0u : kTcLimit);
             if (__syncthreads_or(!ok)) {
                 // flag it, let the MMAs in flight finish (bounded), stop
@@ -350,9 +353,6 @@ __global__ void __launch_bounds__(128 * 2 * H, 1) k_tsp_tc(const TcP P)
             tc_after();
             float dk[CPT];
             tmem_ld<CPT>(tlane, dk);
-            tc_before();
-            __syncthreads();   // colsum, rsum visible; X and TMEM reads done
-            tc_after();
             if (active) {
                 if (H > 1) rs = rsum[m];
 #pragma unroll

@@ -11,7 +11,8 @@
 //   --seed=N         srand seed (default: time(0), as the reference)
 //   --precision=P    f32 (default) | bf16 | f16 | f64
 //   --kernel=K       auto (default) | stream | resident | split (registers +
-//                    shared memory, 16-bit fused state)
+//                    shared memory, 16-bit fused state) | tensor (TSP, 16-bit
+//                    state: the distance product on the tensor cores)
 //   --period=N       steps per window (default: the reference's)
 //   --device=N       CUDA device (default 0)
 //   --compat-stoi    parse time_step with std::stoi as the reference does
@@ -167,6 +168,7 @@ int main(int argc, char *argv[])
             o.kernel = v == "stream"     ? SBX_KERNEL_STREAM
                        : v == "resident" ? SBX_KERNEL_RESIDENT
                        : v == "split"    ? SBX_KERNEL_RESIDENT_SPLIT
+                       : v == "tensor"   ? SBX_KERNEL_TENSOR
                                          : SBX_KERNEL_AUTO;
         else if (k == "period") o.period = std::stoi(v);
         else if (k == "device") o.device = std::stoi(v);
