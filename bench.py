@@ -678,6 +678,15 @@ def main():
                     "launch_us": per_launch_s * 1e6, "launches": rp["kernel_launches"]}
 
     ref_gpu = None
+    if rank == 0 and world == 1 and wl["kind"] == "tsp":
+        import sbo
+        if sbo.ref_gpu_available():
+            rr = sbo.ref_gpu_tsp(oracle_tsp(inst), A, wl["sb_steps"], wl["dt"], seed)
+            ref_gpu = {"value": nnz * A * rr["steps_run"] / (rr["time_us"] / 1e6),
+                       "unit": "nnz*agent*steps/s", "seconds": rr["time_us"] / 1e6,
+                       "best": rr["min"], "valid": rr["valid"], "steps_run": rr["steps_run"],
+                       "kernels": "src/kernels.cu compiled to PTX, driven as src/ising_tsp.cu "
+                                  "drives them (FP64 CSR, its launch shapes, host-clock time)"}
     if rank == 0 and world == 1 and wl["kind"] == "maxcut":
         import sbo
         if sbo.ref_gpu_available():

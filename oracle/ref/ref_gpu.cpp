@@ -1,5 +1,6 @@
 // ref_gpu.cpp -- TEST INFRASTRUCTURE ONLY: runs the reference's own CUDA
-// kernels on the GPU, for the differential against the engine.
+// kernels on the GPU (MaxCut and TSP), for the differential against the
+// engine.
 //
 // The kernels are the reference's src/kernels.cu, compiled to PTX from the
 // reference sources by oracle/Makefile (`ref-ptx`, output oracle/_ref/); this
@@ -48,7 +49,8 @@ int fail(const std::string &m)
 // _Z<length><name><parameters>).
 struct Kernels {
     CUfunction update_xy = nullptr, fused = nullptr, mat_mult = nullptr, confine = nullptr,
-               step_forward = nullptr, window = nullptr, cut = nullptr, sum_cut = nullptr;
+               step_forward = nullptr, window = nullptr, cut = nullptr, sum_cut = nullptr,
+               tsp_step = nullptr, tsp_window = nullptr;
 };
 
 std::string base_name(const char *mangled)
@@ -78,16 +80,198 @@ int find_kernels(CUmodule mod, Kernels &k)
         else if (b == "update_window") k.window = f;
         else if (b == "compute_max_cut") k.cut = f;
         else if (b == "sum_max_cut") k.sum_cut = f;
+        else if (b == "symplectic_kernel_tsp") k.tsp_step = f;
+        else if (b == "update_window_tsp") k.tsp_window = f;
     }
     if (!k.update_xy || !k.fused || !k.mat_mult || !k.confine || !k.step_forward || !k.window || !k.cut ||
-        !k.sum_cut)
+        !k.sum_cut || !k.tsp_step || !k.tsp_window)
         return fail("a reference kernel is missing from the PTX");
+    return 0;
+}
+
+int read_file(const char *path, std::string &out)
+{
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return fail(std::string("cannot open ") + path);
+    char buf[1 << 16];
+    size_t got;
+    while ((got = std::fread(buf, 1, sizeof buf, f)) > 0) out.append(buf, got);
+    std::fclose(f);
     return 0;
 }
 
 }  // namespace
 
 extern "C" const char *ref_gpu_last_error(void) { return g_err.c_str(); }
+
+// One TSP run of the reference's GPU path, as Ising_TSP::reset_initialization
+// + symplectic_update drive it (src/ising_tsp.cu:50-100, 111-248): x = 0 and y
+// from the rand() stream, xi0 = 0.002, n = 2, 32x32 blocks over (agents,
+// rows), the pre-step Update_XY, a captured graph of max_steps / 10
+// symplectic_kernel_tsp launches + update_window_tsp, launched and
+// synchronised until max_steps; then the tours of the valid agents from the
+// final spins (src/ising_tsp.cu:200-215) and their lengths over the packed
+// distances (calculate_distance_of_tour).  The QUBO in CSR and the per-city
+// distance sums are the caller's (the oracle's, pinned to the reference's).
+// stats[8]: loop time in microseconds (the reference's chrono region), min,
+// max, mean, std of the valid tours' lengths, valid agents, SB steps run.
+// lengths[agents] (NaN for agents without a valid tour) is optional.
+extern "C" int ref_gpu_tsp(const char *ptx_path, int device, int ncities, int64_t nnz, const int32_t *rowptr,
+                           const int32_t *col, const double *val, const double *rowsum, const double *packed,
+                           double A, double B, double C, int agents, int max_steps, double dt, unsigned seed,
+                           double *stats, double *lengths)
+{
+    if (!ptx_path || ncities < 3 || agents <= 0 || max_steps < 10 || !rowptr || !col || !val || !rowsum ||
+        !packed || !stats)
+        return fail("bad arguments");
+    const int nrows = ncities * ncities, ncols = agents;
+    const int convergence_threshold = 50;   // src/csr.cuh:167
+    std::string ptx;
+    if (read_file(ptx_path, ptx)) return -1;
+    DRV(cuInit(0));
+    CUdevice dev;
+    DRV(cuDeviceGet(&dev, device));
+    CUcontext ctx;
+    DRV(cuDevicePrimaryCtxRetain(&ctx, dev));
+    DRV(cuCtxPushCurrent(ctx));
+    CUmodule mod = nullptr;
+    CUstream stream = nullptr;
+    CUgraph graph = nullptr;
+    CUgraphExec exec = nullptr;
+    CUdeviceptr d_rp = 0, d_col = 0, d_val = 0, d_rs = 0, d_x = 0, d_y = 0, d_step = 0, d_stab = 0, d_cur = 0,
+                d_fin = 0, d_bif = 0, d_prev = 0, d_valid = 0, d_cv = 0, d_ov = 0;
+    auto body = [&]() -> int {
+        DRV(cuModuleLoadData(&mod, ptx.c_str()));
+        Kernels k;
+        if (find_kernels(mod, k)) return -1;
+        const size_t size = (size_t)nrows * ncols;
+        std::vector<double> X(size, 0.0), Y(size);
+        std::srand(seed);
+        for (size_t i = 0; i < size; i++) Y[i] = (((double)std::rand() / RAND_MAX) * 2 - 1) / 10;
+        DRV(cuMemAlloc(&d_rp, sizeof(int) * (nrows + 1)));
+        DRV(cuMemAlloc(&d_col, sizeof(int) * (nnz > 0 ? nnz : 1)));
+        DRV(cuMemAlloc(&d_val, sizeof(double) * (nnz > 0 ? nnz : 1)));
+        DRV(cuMemAlloc(&d_rs, sizeof(double) * ncities));
+        DRV(cuMemAlloc(&d_x, sizeof(double) * size));
+        DRV(cuMemAlloc(&d_y, sizeof(double) * size));
+        DRV(cuMemAlloc(&d_step, sizeof(int)));
+        DRV(cuMemAlloc(&d_stab, sizeof(int) * size));
+        DRV(cuMemAlloc(&d_cur, sizeof(int) * size));
+        DRV(cuMemAlloc(&d_fin, sizeof(int) * size));
+        DRV(cuMemAlloc(&d_bif, ncols));
+        DRV(cuMemAlloc(&d_prev, ncols));
+        DRV(cuMemAlloc(&d_valid, sizeof(int) * ncols));
+        DRV(cuMemAlloc(&d_cv, sizeof(int) * ncols * ncities));
+        DRV(cuMemAlloc(&d_ov, sizeof(int) * ncols * ncities));
+        DRV(cuMemcpyHtoD(d_rp, rowptr, sizeof(int) * (nrows + 1)));
+        if (nnz > 0) {
+            DRV(cuMemcpyHtoD(d_col, col, sizeof(int) * nnz));
+            DRV(cuMemcpyHtoD(d_val, val, sizeof(double) * nnz));
+        }
+        DRV(cuMemcpyHtoD(d_rs, rowsum, sizeof(double) * ncities));
+        DRV(cuMemcpyHtoD(d_x, X.data(), sizeof(double) * size));
+        DRV(cuMemcpyHtoD(d_y, Y.data(), sizeof(double) * size));
+        DRV(cuMemsetD32(d_step, 0, 1));
+        DRV(cuMemsetD32(d_cur, 0xffffffffu, size));
+        DRV(cuMemsetD32(d_fin, 0xffffffffu, size));
+        DRV(cuMemsetD8(d_bif, 0, ncols));
+        DRV(cuMemsetD8(d_prev, 0, ncols));
+        DRV(cuMemsetD32(d_valid, 0, ncols));
+        DRV(cuMemsetD32(d_cv, 0, (size_t)ncols * ncities));
+        DRV(cuMemsetD32(d_ov, 0, (size_t)ncols * ncities));
+        // the reference never initialises stability; zero it as the oracle
+        // does, so that runs are reproducible where the kernels are
+        DRV(cuMemsetD32(d_stab, 0, size));
+
+        const unsigned gx = (unsigned)((ncols + 31) / 32), gy = (unsigned)((nrows + 31) / 32);
+        int ms = max_steps, nc = ncols, nr = nrows, nci = ncities, thr = convergence_threshold, n2 = 2;
+        double ts = dt, x0 = 0.002, a_ = A, b_ = B, c_ = C;
+        void *a_xy[] = {&d_x, &d_y, &d_step, &ms, &ts, &nc, &nr};
+        void *a_tsp[] = {&d_rp, &d_col, &d_val, &d_rs, &d_x, &d_y, &ts, &d_step, &ms, &x0, &n2,
+                         &a_, &b_, &c_, &nci, &nc, &nr};
+        void *a_win[] = {&d_x, &d_cur, &d_fin, &d_bif, &d_prev, &d_stab, &d_valid, &thr, &d_cv, &d_ov, &d_step,
+                         &nci, &nc, &nr};
+        const int period = max_steps / 10;
+        DRV(cuStreamCreate(&stream, CU_STREAM_NON_BLOCKING));
+        DRV(cuStreamBeginCapture(stream, CU_STREAM_CAPTURE_MODE_GLOBAL));
+        for (int i = 0; i < period; i++)
+            DRV(cuLaunchKernel(k.tsp_step, gx, gy, 1, 32, 32, 1, 0, stream, a_tsp, nullptr));
+        DRV(cuLaunchKernel(k.tsp_window, gx, gy, 1, 32, 32, 1, 0, stream, a_win, nullptr));
+        DRV(cuStreamEndCapture(stream, &graph));
+        DRV(cuGraphInstantiate(&exec, graph, 0));
+        DRV(cuCtxSynchronize());
+
+        const auto t0 = std::chrono::high_resolution_clock::now();
+        DRV(cuLaunchKernel(k.update_xy, gx, gy, 1, 32, 32, 1, 0, nullptr, a_xy, nullptr));
+        DRV(cuCtxSynchronize());
+        int64_t step = 0;
+        bool run = true;
+        while (run) {
+            DRV(cuGraphLaunch(exec, stream));
+            DRV(cuStreamSynchronize(stream));
+            step += period;
+            run = step < max_steps;
+        }
+        const auto t1 = std::chrono::high_resolution_clock::now();
+        const double us = (double)std::chrono::duration_cast<std::chrono::microseconds>(t1 - t0).count();
+
+        std::vector<int> fin(size), valid((size_t)ncols);
+        DRV(cuMemcpyDtoH(fin.data(), d_fin, sizeof(int) * size));
+        DRV(cuMemcpyDtoH(valid.data(), d_valid, sizeof(int) * ncols));
+        // tours of the valid agents and their lengths (src/ising_tsp.cu:
+        // 200-239, calculate_distance_of_tour at :272-287)
+        std::vector<double> all;
+        double total = 0, mn = DBL_MAX, mx = -DBL_MAX;
+        for (int a = 0; a < ncols; a++) {
+            double len = NAN;
+            if (valid[(size_t)a] > 0) {
+                std::vector<int> cities;
+                for (int order = 0; order < ncities; order++)
+                    for (int city = 0; city < ncities; city++)
+                        if (fin[(size_t)(order * ncities + city) * ncols + a] == 1) cities.push_back(city);
+                if ((int)cities.size() != ncities) return fail("a valid agent without a tour");
+                len = 0;
+                for (int i = 0; i < ncities; i++) {
+                    const int u = cities[(size_t)i], v = cities[(size_t)((i + 1) % ncities)];
+                    const int c1 = u < v ? u : v, c2 = u < v ? v : u;
+                    len += packed[c2 + c1 * ncities - (c1 + 2) * (c1 + 1) / 2];
+                }
+                all.push_back(len);
+                total += len;
+                mn = len < mn ? len : mn;
+                mx = len > mx ? len : mx;
+            }
+            if (lengths) lengths[a] = len;
+        }
+        const double avg = total / (double)all.size();
+        double sd = 0;
+        for (double v : all) sd += std::pow(v - avg, 2);
+        stats[0] = us;
+        stats[1] = mn;
+        stats[2] = mx;
+        stats[3] = avg;
+        stats[4] = std::pow(sd / ((double)all.size() - 1), 0.5);
+        stats[5] = (double)all.size();
+        int dstep = 0;
+        DRV(cuMemcpyDtoH(&dstep, d_step, sizeof(int)));
+        stats[6] = dstep;
+        stats[7] = 0;
+        return 0;
+    };
+    const int rc = body();
+    if (exec) cuGraphExecDestroy(exec);
+    if (graph) cuGraphDestroy(graph);
+    if (stream) cuStreamDestroy(stream);
+    CUdeviceptr ptrs[] = {d_rp, d_col, d_val, d_rs, d_x, d_y, d_step, d_stab, d_cur, d_fin, d_bif, d_prev,
+                          d_valid, d_cv, d_ov};
+    for (CUdeviceptr q : ptrs)
+        if (q) cuMemFree(q);
+    if (mod) cuModuleUnload(mod);
+    CUcontext popped;
+    cuCtxPopCurrent(&popped);
+    cuDevicePrimaryCtxRelease(dev);
+    return rc;
+}
 
 // One MaxCut run of the reference's GPU path.  stats[8] receives: SB loop
 // time in microseconds (the reference's chrono region), min, max, mean, std,

@@ -427,3 +427,24 @@ def ref_gpu_maxcut(g, agents, steps, dt, seed, uw=0, fused=1, run_windows=0, wan
     if want_state:
         out.update(x=x, y=y)
     return out
+
+
+def ref_gpu_tsp(t, agents, steps, dt, seed, device=0):
+    """One TSP run of the reference's GPU path (symplectic_kernel_tsp and
+    update_window_tsp in its launch shapes, a graph of steps/10 steps + the
+    window) on the oracle's QUBO and distance sums (pinned to the
+    reference's).  Returns the statistics of the valid agents' tour lengths
+    (time_us is the reference's own host-clock region) and every agent's
+    length (NaN without a valid tour)."""
+    st = np.zeros(8)
+    lengths = np.empty(agents)
+    g = t.graph
+    vp = lambda a: a.ctypes.data_as(C.c_void_p)
+    rc = _ref_lib().ref_gpu_tsp(REF_PTX.encode(), C.c_int(device), C.c_int(t.N), C.c_int64(g.nnz),
+                                vp(g.rowptr), vp(g.col), vp(g.val), vp(t.rowsum), vp(t.packed),
+                                C.c_double(t.qa), C.c_double(t.qb), C.c_double(t.qc), C.c_int(agents),
+                                C.c_int(steps), C.c_double(dt), C.c_uint(seed), vp(st), vp(lengths))
+    if rc != 0:
+        raise RuntimeError("ref_gpu_tsp: " + _ref_lib().ref_gpu_last_error().decode())
+    return {"time_us": st[0], "min": st[1], "max": st[2], "mean": st[3], "std": st[4],
+            "valid": int(st[5]), "steps_run": int(st[6]), "lengths": lengths}

@@ -14,11 +14,12 @@
 // position N holds 0).  X- and X+ are then the same array seen from two start
 // rows 16 apart, two operand descriptors and no copy.  D enters as three
 // 16-bit matrices whose sum is D exactly (hi, mid, lo; FP16 after an exact
-// power-of-two scale), so every product is exact and the sums are FP32 in the
-// tensor core.  Per step one thread issues 12 MMAs (M = 128, N = 32, K = 16)
-// per 128-row tile into TMEM, while every thread sums its column of the
-// state; each thread then reads its row's 32 products back (tcgen05.ld) and
-// updates its spins on the FP32 pipes as the CUDA-core kernel does.
+// power-of-two scale), stacked along N, so every product is exact and the
+// sums are FP32 in the tensor core.  Per step one thread issues 4 MMAs
+// (M = 128, N = 96, K = 16) per 128-row tile into TMEM, while the threads sum
+// the state's columns and rows; each thread then reads its row's products
+// with the three parts back (tcgen05.ld), adds them, and updates its spins on
+// the FP32 pipes as the CUDA-core kernel does.
 //
 // The MMA completion is a bounded mbarrier wait: a wait that runs out flags
 // CTL_ERR, waits (bounded) for the MMAs in flight, frees TMEM and returns.
@@ -87,10 +88,10 @@ template <> struct TcType<__half> {
 };
 
 // instruction descriptor: FP32 accumulator, A and B of the state's type,
-// both K-major, N = 32, M = 128
+// both K-major, N = 96 (the three parts of D stacked), M = 128
 template <class T> __device__ __forceinline__ uint32_t idesc()
 {
-    return (1u << 4) | (TcType<T>::code << 7) | (TcType<T>::code << 10) | ((uint32_t)(NP >> 3) << 17) |
+    return (1u << 4) | (TcType<T>::code << 7) | (TcType<T>::code << 10) | ((uint32_t)(3 * NP >> 3) << 17) |
            ((uint32_t)(128 >> 4) << 24);
 }
 
@@ -218,7 +219,8 @@ __global__ void __launch_bounds__(128 * 2 * H, 1) k_tsp_tc(const TcP P)
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    const uint32_t ncols = 32u * (uint32_t)T2;
+    // TMEM: 96 columns a tile (the products with hi, mid, lo), tile t at 128 t
+    const uint32_t ncols = 128u * (uint32_t)T2;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(&s_tmem)),
                      "r"(ncols));
@@ -280,8 +282,12 @@ __global__ void __launch_bounds__(128 * 2 * H, 1) k_tsp_tc(const TcP P)
     tc_after();
 
     const uint32_t id = idesc<T>();
+    const float qa8u = P.qa8 * P.dunscale;
+    float i2r[CPT];   // the linear field of this thread's cities
+#pragma unroll
+    for (int j = 0; j < CPT; j++) i2r[j] = s_I2[k0 + j];
     // this thread's TMEM lane and its columns
-    const uint32_t tlane = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 32u * (uint32_t)tile + (uint32_t)k0;
+    const uint32_t tlane = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 128u * (uint32_t)tile + (uint32_t)k0;
     const int nwin = P.nwin;
     const uint32_t maskN = N == 32 ? 0xffffffffu : ((1u << N) - 1u);
     int k_step = 0;
@@ -290,21 +296,21 @@ __global__ void __launch_bounds__(128 * 2 * H, 1) k_tsp_tc(const TcP P)
     for (int wdx = 0; wdx < nwin && !failed; wdx++) {
         for (int it = 0; it < P.period; it++, k_step++) {
             const float2 sc = P.sched[k_step];
-            // the distance product of the current X: 12 MMAs per tile
+            // the distance product of the current X: 4 MMAs per tile (both
+            // neighbour positions, two K halves), N = 96 covering the three
+            // parts of D at once
             if (tid == 0) {
                 for (int t = 0; t < T2; t++) {
                     uint32_t acc = 0;
 #pragma unroll
-                    for (int j = 0; j < 3; j++)
+                    for (int h = 0; h < 2; h++)
 #pragma unroll
-                        for (int h = 0; h < 2; h++)
-#pragma unroll
-                            for (int s = 0; s < 2; s++) {
-                                const uint32_t ao = xs0 + (uint32_t)((128 * t + 2 * KA * h) / 8 * SBO + 2 * LBO * s);
-                                const uint32_t bo = ds0 + (uint32_t)(j * DPART + 2 * LBO * s);
-                                mma16(tmem + 32u * (uint32_t)t, sdesc(ao), sdesc(bo), id, acc);
-                                acc = 1;
-                            }
+                        for (int s = 0; s < 2; s++) {
+                            const uint32_t ao = xs0 + (uint32_t)((128 * t + 2 * KA * h) / 8 * SBO + 2 * LBO * s);
+                            const uint32_t bo = ds0 + (uint32_t)(2 * LBO * s);
+                            mma16(tmem + 128u * (uint32_t)t, sdesc(ao), sdesc(bo), id, acc);
+                            acc = 1;
+                        }
                 }
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
                              : "memory");
@@ -316,8 +322,9 @@ __global__ void __launch_bounds__(128 * 2 * H, 1) k_tsp_tc(const TcP P)
             if (active) {
                 if (hh == 0) {
                     float cs = 0.f;
-                    for (int p = 0; p < N; p++)
-                        cs += TT::val(*(const unsigned short *)(xs + opoff((p + 1) * KA + a, i)));
+#pragma unroll
+                    for (int p = 0; p < NP; p++)
+                        if (p < N) cs += TT::val(*(const unsigned short *)(xs + opoff((p + 1) * KA + a, i)));
                     colsum[m] = cs;
                     if (H == 1) {
 #pragma unroll
@@ -351,22 +358,29 @@ __global__ void __launch_bounds__(128 * 2 * H, 1) k_tsp_tc(const TcP P)
             }
             phase ^= 1u;
             tc_after();
-            float dk[CPT];
+            // the products with hi, mid and lo, summed (hi + mid) + lo
+            float dk[CPT], dm[CPT], dl[CPT];
             tmem_ld<CPT>(tlane, dk);
+            tmem_ld<CPT>(tlane + NP, dm);
+            tmem_ld<CPT>(tlane + 2 * NP, dl);
+#pragma unroll
+            for (int j = 0; j < CPT; j++) dk[j] = (dk[j] + dm[j]) + dl[j];
             if (active) {
                 if (H > 1) rs = rsum[m];
 #pragma unroll
                 for (int j = 0; j < CPT; j++) {
                     const int k = k0 + j;
                     if (k < N) {
-                        const float jx = P.qc4 * colsum[k * KA + a] + P.qb4 * rs + P.qa8 * (dk[j] * P.dunscale);
+                        // qa8u = A/8 times the FP16 operand scale 2^s: exact,
+                        // so qa8u * dk is A/8 * (2^s dk) bit for bit
+                        const float jx = P.qc4 * colsum[k * KA + a] + P.qb4 * rs + qa8u * dk[j];
                         float x = xo[j], y = yr[j];
                         if (fabsf(x) > 1.f) {
                             x = spin_of(x);
                             y = 0.f;
                         } else {
                             const float i1 = -1.005f * jx;
-                            y = rnd<T>(y + P.dtxi0 * (2.f * i1 + sc.x * s_I2[k]));
+                            y = rnd<T>(y + P.dtxi0 * (2.f * i1 + sc.x * i2r[j]));
                             x = rnd<T>(x + P.dt * y);
                             y = rnd<T>(y + sc.y * x);
                         }
