@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <chrono>
 #include <cmath>
@@ -171,10 +172,14 @@ void free_csr(DevCsr &J)
     J.perm = nullptr;
 }
 
-// Upload a validated CSR; classify its weights.
+int upload_device(sbx_ctx *ctx, DevCsr &J);
+
+// Validate a CSR, classify its weights and keep it on the host; its device
+// arrays are made by upload_device, at once or -- defer -- when a solve first
+// needs them (a problem that only ever goes into batches never needs its own).
 int upload_csr(sbx_ctx *ctx, DevCsr &J, int64_t n, int64_t nnz, const int32_t *rowptr,
                const int32_t *col, const double *val, double wsum, bool weights_always = false,
-               bool keep_host = true)
+               bool keep_host = true, bool defer = false)
 {
     if (n <= 0 || n > INT32_MAX - 1 || nnz < 0 || nnz > INT32_MAX || !rowptr || (nnz && (!col || !val)))
         return fail(ctx, SBX_ERR_ARG, "bad CSR sizes or pointers");
@@ -243,17 +248,6 @@ int upload_csr(sbx_ctx *ctx, DevCsr &J, int64_t n, int64_t nnz, const int32_t *r
         rowabs_max = std::max(rowabs_max, a.rowabs);
     }
     if (rowabs_max >= 2147483647.0) integer = false;
-    // column words (bit 31: a -1 weight); FP32 weights for other matrices
-    std::vector<uint32_t> colw((size_t)nnz);
-    const bool dev_weights = !unit || weights_always;
-    std::vector<float> valf(dev_weights ? (size_t)nnz : 0);
-    parallel(T, [&](int t, int TT) {
-        const int64_t e0 = nnz * t / TT, e1 = nnz * (t + 1) / TT;
-        for (int64_t e = e0; e < e1; e++) {
-            colw[e] = (uint32_t)col[e] | ((unit && val[e] < 0) ? 0x80000000u : 0u);
-            if (dev_weights) valf[e] = (float)val[e];
-        }
-    });
     // rows by decreasing degree, ties in row order (a counting sort): a warp
     // of the resident kernel gets rows of similar length
     std::vector<int32_t> perm((size_t)n);
@@ -272,12 +266,46 @@ int upload_csr(sbx_ctx *ctx, DevCsr &J, int64_t n, int64_t nnz, const int32_t *r
     J.max_deg = maxdeg;
     J.skewed = (double)maxdeg > 8.0 * std::max(1.0, (double)nnz / (double)n);
     J.niso = niso;
+    J.weights_always = weights_always;
     if (keep_host) {   // else the caller moves its arrays in
         J.hval.assign(val, val + nnz);
         J.hrowptr.assign(rowptr, rowptr + n + 1);
         J.hcol.assign(col, col + nnz);
     }
-    J.hperm = perm;
+    J.hperm = std::move(perm);
+    // heavy rows (+-1, more than kHeavy neighbours) in chunks of kHeavy
+    J.nheavy = 0;
+    J.nchunks = 0;
+    if (unit && maxdeg > kHeavy)
+        for (int64_t r = 0; r < n; r++) {
+            const int32_t deg = rowptr[r + 1] - rowptr[r];
+            if (deg <= kHeavy) continue;
+            J.nheavy++;
+            J.nchunks += (deg + kHeavy - 1) / kHeavy;
+        }
+    return defer ? SBX_OK : upload_device(ctx, J);
+}
+
+// The device arrays of a CSR from its host copies: row pointers, column
+// words (bit 31: a -1 weight), FP32/FP64 weights where the kernels read
+// them, the degree order and the heavy rows' chunks.
+int upload_device(sbx_ctx *ctx, DevCsr &J)
+{
+    if (J.rowptr) return SBX_OK;
+    const int64_t n = J.n, nnz = J.nnz;
+    const int32_t *rowptr = J.hrowptr.data(), *col = J.hcol.data();
+    const double *val = J.hval.data();
+    const int T = nnz > (1 << 20) ? host_threads() : 1;
+    std::vector<uint32_t> colw((size_t)nnz);
+    const bool dev_weights = !J.unit || J.weights_always;
+    std::vector<float> valf(dev_weights ? (size_t)nnz : 0);
+    parallel(T, [&](int t, int TT) {
+        const int64_t e0 = nnz * t / TT, e1 = nnz * (t + 1) / TT;
+        for (int64_t e = e0; e < e1; e++) {
+            colw[e] = (uint32_t)col[e] | ((J.unit && val[e] < 0) ? 0x80000000u : 0u);
+            if (dev_weights) valf[e] = (float)val[e];
+        }
+    });
     CK(cudaMalloc(&J.rowptr, sizeof(int32_t) * (n + 1)));
     CK(cudaMalloc(&J.colw, sizeof(uint32_t) * std::max<int64_t>(nnz, 1)));
     CK(cudaMalloc(&J.perm, sizeof(int32_t) * n));
@@ -294,17 +322,16 @@ int upload_csr(sbx_ctx *ctx, DevCsr &J, int64_t n, int64_t nnz, const int32_t *r
             CK(cudaMemcpy(J.valf, valf.data(), sizeof(float) * nnz, cudaMemcpyHostToDevice));
         }
     }
-    CK(cudaMemcpy(J.perm, perm.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
-    if (unit && maxdeg > kHeavy) {
+    CK(cudaMemcpy(J.perm, J.hperm.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+    if (J.nchunks) {
         std::vector<int32_t> hchunk((size_t)n, -1), crow;
+        crow.reserve((size_t)J.nchunks);
         for (int64_t r = 0; r < n; r++) {
             const int32_t deg = rowptr[r + 1] - rowptr[r];
             if (deg <= kHeavy) continue;
             hchunk[r] = (int32_t)crow.size();
             for (int32_t c = 0; c < (deg + kHeavy - 1) / kHeavy; c++) crow.push_back((int32_t)r);
         }
-        J.nchunks = (int32_t)crow.size();
-        for (int64_t r = 0; r < n; r++) J.nheavy += hchunk[r] >= 0;
         CK(cudaMalloc(&J.hchunk, sizeof(int32_t) * n));
         CK(cudaMalloc(&J.chunk_row, sizeof(int32_t) * crow.size()));
         CK(cudaMemcpy(J.hchunk, hchunk.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
@@ -706,6 +733,9 @@ int ensure_rs_csr(sbx_ctx *ctx, DevCsr &J);
 int solve_maxcut(sbx_ctx *ctx, const sbx_problem *p, const sbx_params *pr, sbx_result *res,
                  double *agent_values)
 {
+    // the problem's device arrays, made on its first single solve
+    int urc = upload_device(ctx, const_cast<DevCsr &>(p->J));
+    if (urc) return urc;
     SolveDims d;
     d.n = p->J.n;
     d.A = pr->agents;
@@ -1035,11 +1065,12 @@ int build_class(sbx_ctx *ctx, BatchClass &c)
         }
     });
     rp[n] = (int32_t)nnz;
-    int rc = upload_csr(ctx, c.J, n, nnz, rp.data(), col.data(), val.data(), 0.0, false, false);
+    int rc = upload_csr(ctx, c.J, n, nnz, rp.data(), col.data(), val.data(), 0.0, false, false, true);
     if (rc) return rc;
     c.J.hrowptr = std::move(rp);
     c.J.hcol = std::move(col);
     c.J.hval = std::move(val);
+    if ((rc = upload_device(ctx, c.J))) return rc;
     CK(cudaMalloc(&c.J.rinst, sizeof(int32_t) * n));
     CK(cudaMalloc(&c.J.c0r32, sizeof(float) * n));
     CK(cudaMalloc(&c.J.c0r64, sizeof(double) * n));
@@ -1170,25 +1201,36 @@ int build_bsm(sbx_ctx *ctx, BatchClass &c, int W)
     std::vector<int32_t> ioff(ni), in(ni);
     int64_t maxn = 0;
     for (size_t i = 0; i < ni; i++) {
-        const int64_t r0 = c.row_off[i], rn = c.probs[i]->J.n;
-        ioff[i] = (int32_t)r0;
-        in[i] = (int32_t)rn;
-        maxn = std::max(maxn, rn);
-        if (rn > 32767) return fail(ctx, SBX_ERR_UNSUPPORTED, "batch: shared-plane kernel instance too large");
-        const uint16_t zrow = (uint16_t)rn;
-        for (int64_t r = r0; r < r0 + rn; r++) {
-            int64_t o = (int64_t)(rinfo[(size_t)r] >> 7) * 8;
-            const int64_t e1 = c.J.hrowptr[(size_t)r + 1];
-            for (int64_t e = c.J.hrowptr[(size_t)r]; e < e1; e++) {
-                const int64_t lc = (int64_t)c.J.hcol[(size_t)e] - r0;
-                // the kernel reads the plane at this offset: it must be a row
-                // of the instance (a block-diagonal matrix guarantees it)
-                if (lc < 0 || lc >= rn) return fail(ctx, SBX_ERR_ARG, "batch: a column outside its instance");
-                lcol[(size_t)o++] = (uint16_t)((uint32_t)lc | (c.J.hval[(size_t)e] < 0 ? 0x8000u : 0u));
-            }
-            while (o & 7) lcol[(size_t)o++] = zrow;
-        }
+        ioff[i] = (int32_t)c.row_off[i];
+        in[i] = (int32_t)c.probs[i]->J.n;
+        maxn = std::max<int64_t>(maxn, in[i]);
+        if (in[i] > 32767) return fail(ctx, SBX_ERR_UNSUPPORTED, "batch: shared-plane kernel instance too large");
     }
+    // the instances' blocks on host threads (disjoint ranges of lcol)
+    std::atomic<int> outside(0);
+    parallel(c.J.nnz > (1 << 20) ? host_threads() : 1, [&](int t, int TT) {
+        for (size_t i = (size_t)t; i < ni; i += (size_t)TT) {
+            const int64_t r0 = ioff[i], rn = in[i];
+            const uint16_t zrow = (uint16_t)rn;
+            for (int64_t r = r0; r < r0 + rn; r++) {
+                int64_t o = (int64_t)(rinfo[(size_t)r] >> 7) * 8;
+                const int64_t e1 = c.J.hrowptr[(size_t)r + 1];
+                for (int64_t e = c.J.hrowptr[(size_t)r]; e < e1; e++) {
+                    const int64_t lc = (int64_t)c.J.hcol[(size_t)e] - r0;
+                    // the kernel reads the plane at this offset: it must be
+                    // a row of the instance (a block-diagonal matrix
+                    // guarantees it)
+                    if (lc < 0 || lc >= rn) {
+                        outside = 1;
+                        return;
+                    }
+                    lcol[(size_t)o++] = (uint16_t)((uint32_t)lc | (c.J.hval[(size_t)e] < 0 ? 0x8000u : 0u));
+                }
+                while (o & 7) lcol[(size_t)o++] = zrow;
+            }
+        }
+    });
+    if (outside) return fail(ctx, SBX_ERR_ARG, "batch: a column outside its instance");
     const int grid = std::max(1, dev_attr(cudaDevAttrMultiProcessorCount));
     const double row_cost = 16.0 * W + 16.0;
     double total = 0;
@@ -1792,7 +1834,7 @@ int sbx_problem_csr(sbx_ctx *ctx, int64_t n, int64_t nnz, const int32_t *rowptr,
     CK(cudaSetDevice(ctx->device));
     sbx_problem *p = new sbx_problem;
     p->ctx = ctx;
-    int rc = upload_csr(ctx, p->J, n, nnz, rowptr, col, val, weight_sum);
+    int rc = upload_csr(ctx, p->J, n, nnz, rowptr, col, val, weight_sum, false, true, true);
     if (rc) {
         free_csr(p->J);
         delete p;

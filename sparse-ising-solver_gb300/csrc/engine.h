@@ -70,6 +70,7 @@ struct DevCsr {
     int32_t ninst = 0;
     int32_t *iagents = nullptr;
     double *iwsum = nullptr;
+    bool weights_always = false;  // the device copy holds the weights even when all are +-1
     bool unit = false;       // all |w| == 1
     bool allpos = false;     // all w == +1 (unit, no sign bits)
     bool integer = false;    // all integer-valued, small enough for int32 sums
