@@ -73,8 +73,12 @@ TRAFFIC = {
     # per SB step: the k_row launch plus 1/100 of the isolated rows' k_iso
     "rmat20": (9.814e8, "ncu --set full -k regex:k_row|k_iso: bench.py --workload rmat20 "
                         "--profile 100 (k_row launch + k_iso / 100)"),
-    "batch512": (1.3268e9, "ncu --set full -k regex:k_row -s 4 -c 1: bench.py --workload batch512 "
-                           "--profile 100 --tile 8,8,128,2"),
+    "batch512": (1.0659e9, "ncu --set full -k regex:k_bsm -s 4 -c 1: bench.py --workload batch512 "
+                           "--profile 100 (one k_bsm launch)"),
+    # the whole 2,000-step solve is one launch; per launch of the bench's
+    # 20,000-step solve the state read once is the same
+    "tsp30": (3.870e6, "ncu --set full -k regex:k_tsp_tc -c 1: bench.py --workload tsp30 "
+                       "--profile 2000 --kernel tensor --precision bf16 (one launch)"),
 }
 
 
