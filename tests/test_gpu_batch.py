@@ -87,3 +87,21 @@ def test_shared_plane_and_streaming_batch_kernels_agree(ctx):
     assert np.array_equal(v4, v2)
     for p in probs:
         p.close()
+
+
+def test_instances_past_the_16_bit_columns_take_the_streaming_kernel(ctx, oracle):
+    # An instance of more than 32,767 rows cannot be addressed by the
+    # shared-plane kernel's 16-bit columns (at 32 agents its 132 KB plane
+    # would fit in shared memory): the batch runs on the streaming kernel
+    # instead (bit-exact with the oracle), and asking for count mode 4 is
+    # refused with the reason.
+    graphs = [sbx.gen_er(33000, 0.0002, pm1=True, seed=8), sbx.gen_rgg(500, 9.0, seed=9)]
+    res = _check(ctx, oracle, graphs, 32, sbx.BF16, 1, run=100, steps=2000)
+    assert res[0]["count_mode"] != 4
+    probs = [ctx.problem(g) for g in graphs]
+    with pytest.raises(sbx.SbxError) as e:
+        ctx.solve_batch(probs, [32, 32], sbx.params(dt=0.5, steps=200, seed=1, precision=sbx.BF16,
+                                                   count_mode=4))
+    assert e.value.rc == sbx.ERR_UNSUPPORTED
+    for p in probs:
+        p.close()
