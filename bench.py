@@ -52,8 +52,8 @@ WORKLOADS = {
     # fixed xi0 = 0.002 (ising_tsp.cu:61) suits TSPLIB-sized distances; at
     # unit scale its dynamics find no valid tour (checked with the oracle)
     "tsp30": dict(kind="tsp", workload="tsp-30-unit-square-x1000-penalty1.5maxd", cities=30,
-                  coord_scale=1000.0, agents=1024, dt=0.1, sb_steps=20000, precision="bf16",
-                  compare=("f16", "f32", "f64")),
+                  coord_scale=1000.0, agents=1024, dt=0.1, sb_steps=20000, precision="f16",
+                  compare=("bf16", "f32", "f64")),
     "loaders": dict(kind="loaders", workload="loaders", sb_steps=0),
     "batch512": dict(kind="batch", workload="batch-512-maxcut-er+rgg-n100..20000-pm1",
                      instances=512, agents=64, dt=0.5, sb_steps=10000, fused=1,

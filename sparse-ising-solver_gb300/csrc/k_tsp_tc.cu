@@ -170,6 +170,14 @@ template <> __device__ __forceinline__ void tmem_ld<8>(uint32_t ta, float *v)
 
 template <class T> __device__ __forceinline__ float rnd(float v) { return St<T>::ld(St<T>::st(v)); }
 
+// two values rounded to the storage type and back (one packed conversion)
+template <class T> __device__ __forceinline__ float2 rnd2(float2 v);
+template <> __device__ __forceinline__ float2 rnd2<__nv_bfloat16>(float2 v)
+{
+    return __bfloat1622float2(__float22bfloat162_rn(v));
+}
+template <> __device__ __forceinline__ float2 rnd2<__half>(float2 v) { return __half22float2(__float22half2_rn(v)); }
+
 // H threads share a row m = (i, a): thread part hh owns the cities
 // [32 hh / H, 32 (hh + 1) / H).  Warp w reads TMEM lanes 32 (w mod 4) of
 // tile (w / 4) mod T, part (w / 4) / T; 128 T H threads.
@@ -367,25 +375,38 @@ __global__ void __launch_bounds__(128 * 2 * H, 1) k_tsp_tc(const TcP P)
             for (int j = 0; j < CPT; j++) dk[j] = (dk[j] + dm[j]) + dl[j];
             if (active) {
                 if (H > 1) rs = rsum[m];
+                // two cities at a time in packed FP32 (per component the
+                // roundings of fmaf / __fmul_rn), both clamp branches
+                // computed and selected; cities past N stay zero
+                const float2 qc = make_float2(P.qc4, P.qc4), qb = make_float2(P.qb4, P.qb4);
+                const float2 rs2 = make_float2(rs, rs);
+                const float2 qa = make_float2(qa8u, qa8u), m1005 = make_float2(-1.005f, -1.005f);
+                const float2 two = make_float2(2.f, 2.f), bt = make_float2(sc.x, sc.x);
+                const float2 cxi = make_float2(P.dtxi0, P.dtxi0), cdt = make_float2(P.dt, P.dt);
+                const float2 cy = make_float2(sc.y, sc.y);
 #pragma unroll
-                for (int j = 0; j < CPT; j++) {
+                for (int j = 0; j < CPT; j += 2) {
                     const int k = k0 + j;
+                    const float2 cs2 = make_float2(colsum[k * KA + a], colsum[(k + 1) * KA + a]);
+                    // jx = (qc4 colsum + qb4 rs) + qa8u dk as the CUDA-core
+                    // kernel contracts it; qa8u = A/8 times the FP16 operand
+                    // scale 2^s (exact), so qa8u dk is A/8 (2^s dk) bit for bit
+                    const float2 jx = __ffma2_rn(qa, make_float2(dk[j], dk[j + 1]),
+                                                 __ffma2_rn(qb, rs2, __fmul2_rn(qc, cs2)));
+                    const float2 i1 = __fmul2_rn(m1005, jx);
+                    const float2 x0 = make_float2(xo[j], xo[j + 1]), y0 = make_float2(yr[j], yr[j + 1]);
+                    float2 y = rnd2<T>(__ffma2_rn(cxi, __ffma2_rn(bt, make_float2(i2r[j], i2r[j + 1]),
+                                                                   __fmul2_rn(two, i1)), y0));
+                    const float2 x = rnd2<T>(__ffma2_rn(cdt, y, x0));
+                    y = rnd2<T>(__ffma2_rn(cy, x, y));
+                    const bool c0 = fabsf(x0.x) > 1.f, c1 = fabsf(x0.y) > 1.f;
                     if (k < N) {
-                        // qa8u = A/8 times the FP16 operand scale 2^s: exact,
-                        // so qa8u * dk is A/8 * (2^s dk) bit for bit
-                        const float jx = P.qc4 * colsum[k * KA + a] + P.qb4 * rs + qa8u * dk[j];
-                        float x = xo[j], y = yr[j];
-                        if (fabsf(x) > 1.f) {
-                            x = spin_of(x);
-                            y = 0.f;
-                        } else {
-                            const float i1 = -1.005f * jx;
-                            y = rnd<T>(y + P.dtxi0 * (2.f * i1 + sc.x * i2r[j]));
-                            x = rnd<T>(x + P.dt * y);
-                            y = rnd<T>(y + sc.y * x);
-                        }
-                        xo[j] = x;
-                        yr[j] = y;
+                        xo[j] = c0 ? spin_of(x0.x) : x.x;
+                        yr[j] = c0 ? 0.f : y.x;
+                    }
+                    if (k + 1 < N) {
+                        xo[j + 1] = c1 ? spin_of(x0.y) : x.y;
+                        yr[j + 1] = c1 ? 0.f : y.y;
                     }
                 }
                 put_row();
