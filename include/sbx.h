@@ -100,7 +100,8 @@ typedef struct sbx_params {
                                4 (batched, 16-bit state, 32/64/128 agents,
                                degree <= 127) each instance's sign plane in
                                shared memory, a lane per 32-agent word --
-                               block_threads 512 or 1024 sets its CTA size;
+                               block_threads 512, 640 (default) or 1024
+                               sets its CTA size;
                                0: autotuned (batches that fit take 4) */
     int32_t staging;        /* state larger than L2, whole-warp rows: 1 direct
                                loads, 2 rows copied ahead into shared memory

@@ -1496,7 +1496,7 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
         const bool use_rb = want_rb && rb_ok;
         // the shared-memory-plane step kernel, unless a streaming tile or
         // another count mode is asked for (count_mode 4 insists on it)
-        const bool bsm_threads = pr->block_threads == 512 || pr->block_threads == 1024;
+        const bool bsm_threads = pr->block_threads == 512 || pr->block_threads == 640 || pr->block_threads == 1024;
         const bool tile_pinned = pr->lane_agents || pr->row_lanes || (pr->block_threads && !bsm_threads) ||
                                  pr->staging || (pr->count_mode && pr->count_mode != 4);
         const bool bsm_fit = !use_rb && bsm_ok(c, d);
@@ -1515,9 +1515,9 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
         } else if (use_bsm) {
             if (!c.bsm.lcol && (rc = build_bsm(ctx, c, d.W))) return rc;
             c.J.bsm = &c.bsm;
-            // 512 threads (128 registers each) measured 1.5% faster than 1024
-            // on GB300 (batch512: 292 against 297 us a step)
-            d.tbsm = bsm_threads ? pr->block_threads : 512;
+            // 640 threads (96 registers each) measured fastest on GB300
+            // (batch512: 257 us a step against 271 with 512 and 277 with 1024)
+            d.tbsm = bsm_threads ? pr->block_threads : 640;
         } else if (nchunks) {
             bool timed = false;
             if ((rc = pick_tile(ctx, d, c.J, pr, &timed))) return rc;

@@ -263,12 +263,13 @@ cudaError_t launch_n(const StepP &P, const BsmP &B, int grid, size_t smem, int o
     return launch(kern, dim3((unsigned)grid), dim3(NT), smem, s, pdl, P, B, offset);
 }
 
-// CTA size: 1024 threads (64 registers each) or 512 (128 registers)
+// CTA size: 1024 threads (64 registers each), 640 (96) or 512 (128)
 template <class T, int W, int KIND, bool WIN>
 cudaError_t launch_w(const StepP &P, const BsmP &B, int grid, size_t smem, int offset, cudaStream_t s,
                      bool pdl, int nt)
 {
     if (nt == 512) return launch_n<T, W, KIND, WIN, 512>(P, B, grid, smem, offset, s, pdl);
+    if (nt == 640) return launch_n<T, W, KIND, WIN, 640>(P, B, grid, smem, offset, s, pdl);
     return launch_n<T, W, KIND, WIN, 1024>(P, B, grid, smem, offset, s, pdl);
 }
 
@@ -312,7 +313,7 @@ cudaError_t launch_batch_smem(const SolveDims &d, const DevBsm &M, const StepP &
     B.ioff = M.ioff;
     B.in = M.in;
     const size_t smem = bsm_smem_bytes(M.max_rows, d.W);
-    const int nt = d.tbsm == 512 ? 512 : 1024;
+    const int nt = d.tbsm == 512 || d.tbsm == 640 ? d.tbsm : 1024;
     if (d.prec == P_BF16) return launch_k<__nv_bfloat16>(kind, win, d.W, P, B, M.grid, smem, offset, s, d.pdl, nt);
     if (d.prec == P_F16) return launch_k<__half>(kind, win, d.W, P, B, M.grid, smem, offset, s, d.pdl, nt);
     return cudaErrorInvalidValue;

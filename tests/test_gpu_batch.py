@@ -70,7 +70,7 @@ def test_shared_plane_kernel_all_positive_weights(ctx, oracle):
     assert res[0]["count_mode"] == 4
 
 
-@pytest.mark.parametrize("threads", [512, 1024])
+@pytest.mark.parametrize("threads", [512, 640, 1024])
 def test_shared_plane_kernel_cta_sizes_agree(ctx, oracle, threads):
     res = _check(ctx, oracle, _graphs(), 64, sbx.BF16, 1, count_mode=4, block_threads=threads)
     assert res[0]["count_mode"] == 4 and res[0]["block_threads"] == threads

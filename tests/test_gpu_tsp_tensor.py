@@ -52,10 +52,13 @@ def _run(ctx, prob, N, A, prec, kernel, **kw):
 
 
 @pytest.mark.parametrize("prec", [sbx.BF16, sbx.F16])
-@pytest.mark.parametrize("N,scale", [(12, 1000.0), (30, 1000.0), (17, 3.0e6)])
+@pytest.mark.parametrize("N,scale", [(3, 1000.0), (12, 1000.0), (16, 1000.0), (30, 1000.0),
+                                     (32, 1000.0), (17, 3.0e6)])
 def test_one_step_within_one_ulp_of_cuda_core(ctx, prec, N, scale):
-    # (17, 3e6): distances far past FP16's range, so the FP16 operands are
-    # scaled; 17 cities and 8 agents per CTA leave rows of the second tile idle
+    # 3 cities: the smallest the kernel takes; 16: one full 128-row tile;
+    # 32: two full tiles and every bit of the 32-city masks; (17, 3e6):
+    # distances far past FP16's range, so the FP16 operands are scaled, and
+    # 17 cities with 8 agents per CTA leave rows of the second tile idle
     prob, _ = _problem(ctx, N, scale, seed=N)
     A = 72   # not a multiple of 8: the last CTA holds padded agents
     kw = dict(dt=0.1, steps=1000, run_steps=1, period=1, seed=9)
