@@ -61,6 +61,8 @@ WORKLOADS = {
 }
 GRAPH_SEED, INIT_SEED = 1234, 1
 PBYTES = {"f32": 4, "bf16": 2, "f16": 2, "f64": 8}
+# time to target with restarts: copies of each missed instance per round
+RESTART_COPIES = 4
 
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of
@@ -892,26 +894,31 @@ def run_batch(args, wl, rank, world, local):
         tp.append(r["time_to_target_us"])
     tp = np.array(tp)
     reached = tb > 0
-    # Restarts: the instances the batch missed are solved again, as a smaller
-    # batch from other seeds, until every instance has reached its target
-    # (at most 6 rounds).  The first round counts whole (its misses are known
-    # only at its end), so does every round that still misses one; the round
-    # that reaches the last targets counts up to its slowest instance.
+    # Restarts: the instances the batch missed are solved again from other
+    # seeds, RESTART_COPIES copies of each in one smaller batch (every copy
+    # has its own seed, the batch seeding entry k with seed + k), until every
+    # instance has reached its target (at most 6 rounds).  An instance is
+    # reached in a round when one of its copies is, at that copy's time.  The
+    # first round counts whole (its misses are known only at its end), so does
+    # every round that still misses one; the round that reaches the last
+    # targets counts up to its slowest instance.
     t_restart = float(np.max(tb)) if reached.all() else None
     rounds, missed = 0, np.nonzero(~reached)[0]
-    left = [int(len(missed))]
+    left, round_us = [int(len(missed))], []
     if not reached.all():
-        t_restart = t_first = float(rt[0]["time_us"]) if rt[0]["time_us"] > 0 else None
-        t_restart = t_first
+        t_restart = float(rt[0]["time_us"]) if rt[0]["time_us"] > 0 else None
         while len(missed) and rounds < 6 and t_restart is not None:
             rounds += 1
-            sub = [probs[i] for i in missed]
-            rr, _, t_sub = ctx.solve_batch(sub, [A] * len(sub), sbx.params(
+            rep = np.repeat(missed, RESTART_COPIES)
+            rr, _, t_sub = ctx.solve_batch([probs[i] for i in rep], [A] * len(rep), sbx.params(
                 dt=wl["dt"], steps=wl["sb_steps"], seed=seed + 7919 * rounds, fused=wl["fused"],
-                precision=sbx.PRECISIONS[wl["precision"]]), targets=targets[missed])
-            tr_ = np.array([r["time_to_target_us"] for r in rr])
-            ok = tr_ > 0
-            t_restart += float(tr_.max()) if ok.all() else float(t_sub)
+                precision=sbx.PRECISIONS[wl["precision"]]), targets=targets[rep])
+            tr_ = np.array([r["time_to_target_us"] for r in rr]).reshape(len(missed), RESTART_COPIES)
+            hit = np.where(tr_ > 0, tr_, np.inf).min(axis=1)
+            ok = np.isfinite(hit)
+            t_round = float(hit.max()) if ok.all() else float(t_sub)
+            t_restart += t_round
+            round_us.append(t_round)
             missed = missed[~ok]
             left.append(int(len(missed)))
         if len(missed):
@@ -924,7 +931,10 @@ def run_batch(args, wl, rank, world, local):
            "speedup": float(tp.sum() / tb.max()) if reached.all() else None,
            "missed": [int(i) for i in np.nonzero(~reached)[0]],
            "with_restarts": {"rounds": rounds, "all_reached": t_restart is not None,
+                             "copies_per_round": RESTART_COPIES,
                              "missed_after_each_round": left,
+                             "round_us": round_us,
+                             "missed_rows": [int(graphs[i].n) for i in missed],
                              "batched_us": t_restart,
                              "speedup": float(tp.sum() / t_restart) if t_restart else None}}
     peaks, peak_kind = load_peaks()

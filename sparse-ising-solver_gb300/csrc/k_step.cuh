@@ -520,10 +520,11 @@ __device__ __forceinline__ void sb_update(double (&x)[V], double (&y)[V], const 
 // P.bits_min or more neighbours are counted in bit planes (mixed mode).
 // Isolated rows (the last P.niso entries of the order) are left to k_iso.
 // Resident CTAs per SM asked of the register allocator (measured on GB300):
-// 6 for heavy-row kernels, 4 for bit-plane counting (its loads in flight
-// need registers), 5 otherwise.
+// 4 for bit-plane counting without heavy rows (its loads in flight need
+// registers), 5 otherwise (heavy-row kernels: 6 spilled more and ran 2%
+// slower on R-MAT 2^20, 7 ran 11% slower).
 template <class T, int V, int KIND, bool WIN, int WM, bool BIG, int LR, int CM, int ST>
-__global__ void __launch_bounds__(256, BIG ? 6 : (CM ? 4 : 5)) k_row(const StepP P, const int offset)
+__global__ void __launch_bounds__(256, (CM && !BIG) ? 4 : 5) k_row(const StepP P, const int offset)
 {
     static_assert(LR == 32 || !BIG, "heavy rows are counted by whole warps");
     static_assert(!ST || (LR == 32 && !WIN && KIND != K_XY), "staged rows: whole-warp rows, plain steps");

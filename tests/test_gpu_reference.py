@@ -66,13 +66,15 @@ def test_reference_gpu_whole_run_and_engine_fp32_plain(oracle_ref, name):
 
 
 def test_reference_gpu_tsp_whole_run_and_engine(oracle_ref):
-    # TSP with 30 cities and 1024 agents (the TSP workload, 4,000 steps): the
-    # reference's kernels (FP64, X updated in place) and the engine's FP64
-    # and BF16 tensor-core runs from the same seed find valid tours of
-    # comparable length; every tour length the reference reports is the
-    # oracle's length of some permutation (checked by its range).
+    # TSP with 30 cities and 1024 agents (the TSP workload, its 20,000
+    # steps): the reference's kernels (FP64, X updated in place) and the
+    # engine's FP64 run and FP16 / BF16 tensor-core runs from the same seed
+    # find valid tours of comparable length.  The best of 1024 agents is
+    # still noisy at a fifth of the steps: BF16 state (8-bit mantissa) ended
+    # 6.7% above the reference's best at 4,000 steps, while at 20,000 steps
+    # all of them lie within 1%.
     oracle = oracle_ref
-    wl = dict(bench.WORKLOADS["tsp30"], sb_steps=4000)
+    wl = dict(bench.WORKLOADS["tsp30"])
     inst = bench.build_instance(wl, oracle)
     t = bench.oracle_tsp(inst)
     A, steps, dt = wl["agents"], wl["sb_steps"], wl["dt"]
@@ -81,7 +83,7 @@ def test_reference_gpu_tsp_whole_run_and_engine(oracle_ref):
     assert r["valid"] > 0 and np.isfinite(r["min"])
     ctx = sbx.Context(0)
     prob = ctx.tsp_problem(inst["packed"], inst["N"], A=inst["A"], B=inst["B"], C_=inst["C"])
-    for prec in (sbx.F64, sbx.BF16):
+    for prec in (sbx.F64, sbx.F16, sbx.BF16):
         e, lengths = ctx.solve(prob, sbx.params(dt=dt, steps=steps, agents=A, seed=1, precision=prec))
         assert e["valid"] > 0
         # within 5% of the reference's best tour (different trajectories)
