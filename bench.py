@@ -61,8 +61,11 @@ WORKLOADS = {
 }
 GRAPH_SEED, INIT_SEED = 1234, 1
 PBYTES = {"f32": 4, "bf16": 2, "f16": 2, "f64": 8}
-# time to target with restarts: copies of each missed instance per round
-RESTART_COPIES = 4
+# time to target with restarts: each restart round solves copies of the
+# missed instances, as many as keep the round's batch near this share of the
+# full batch's rows (at least one copy, at most RESTART_MAX_COPIES)
+RESTART_ROWS = 0.1
+RESTART_MAX_COPIES = 32
 
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of
@@ -895,25 +898,30 @@ def run_batch(args, wl, rank, world, local):
     tp = np.array(tp)
     reached = tb > 0
     # Restarts: the instances the batch missed are solved again from other
-    # seeds, RESTART_COPIES copies of each in one smaller batch (every copy
-    # has its own seed, the batch seeding entry k with seed + k), until every
-    # instance has reached its target (at most 6 rounds).  An instance is
-    # reached in a round when one of its copies is, at that copy's time.  The
-    # first round counts whole (its misses are known only at its end), so does
-    # every round that still misses one; the round that reaches the last
-    # targets counts up to its slowest instance.
+    # seeds, several copies of each in one smaller batch (every copy has its
+    # own seed, the batch seeding entry k with seed + k; the copy count keeps
+    # the round near RESTART_ROWS of the full batch's rows, so a round costs
+    # about a tenth of the first and the last few instances get many seeds),
+    # until every instance has reached its target (at most 8 rounds).  An
+    # instance is reached in a round when one of its copies is, at that
+    # copy's time.  The first round counts whole (its misses are known only
+    # at its end), so does every round that still misses one; the round that
+    # reaches the last targets counts up to its slowest instance.
     t_restart = float(np.max(tb)) if reached.all() else None
     rounds, missed = 0, np.nonzero(~reached)[0]
-    left, round_us = [int(len(missed))], []
+    left, round_us, copies_used = [int(len(missed))], [], []
     if not reached.all():
         t_restart = float(rt[0]["time_us"]) if rt[0]["time_us"] > 0 else None
-        while len(missed) and rounds < 6 and t_restart is not None:
+        while len(missed) and rounds < 8 and t_restart is not None:
             rounds += 1
-            rep = np.repeat(missed, RESTART_COPIES)
+            rows_missed = sum(graphs[i].n for i in missed)
+            copies = int(min(RESTART_MAX_COPIES, max(1, RESTART_ROWS * n_tot // rows_missed)))
+            copies_used.append(copies)
+            rep = np.repeat(missed, copies)
             rr, _, t_sub = ctx.solve_batch([probs[i] for i in rep], [A] * len(rep), sbx.params(
-                dt=wl["dt"], steps=wl["sb_steps"], seed=seed + 7919 * rounds, fused=wl["fused"],
+                dt=wl["dt"], steps=wl["sb_steps"], seed=seed + 100000 * rounds, fused=wl["fused"],
                 precision=sbx.PRECISIONS[wl["precision"]]), targets=targets[rep])
-            tr_ = np.array([r["time_to_target_us"] for r in rr]).reshape(len(missed), RESTART_COPIES)
+            tr_ = np.array([r["time_to_target_us"] for r in rr]).reshape(len(missed), copies)
             hit = np.where(tr_ > 0, tr_, np.inf).min(axis=1)
             ok = np.isfinite(hit)
             t_round = float(hit.max()) if ok.all() else float(t_sub)
@@ -931,7 +939,7 @@ def run_batch(args, wl, rank, world, local):
            "speedup": float(tp.sum() / tb.max()) if reached.all() else None,
            "missed": [int(i) for i in np.nonzero(~reached)[0]],
            "with_restarts": {"rounds": rounds, "all_reached": t_restart is not None,
-                             "copies_per_round": RESTART_COPIES,
+                             "copies_per_round": copies_used,
                              "missed_after_each_round": left,
                              "round_us": round_us,
                              "missed_rows": [int(graphs[i].n) for i in missed],
