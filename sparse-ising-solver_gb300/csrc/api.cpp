@@ -56,6 +56,10 @@ struct BatchClass {
     DevBsm bsm;                           // plan of the shared-memory-plane step (on first use)
     std::vector<int32_t> agent_off;       // instance i's cuts at [agent_off[i], agent_off[i + 1])
     int32_t *daoff = nullptr;             // the same on the device
+    // Each instance's rows are renumbered by decreasing degree inside its
+    // block: slot[row_off + r] is the class row of the instance's row r.
+    std::vector<int32_t> slot;
+    int32_t *dslot = nullptr;             // the same on the device (the init writes through it)
 };
 
 struct sbx_ctx {
@@ -424,8 +428,10 @@ constexpr int kRandBits = 40;             // jump matrices kept: 2^40 threads
 
 // x, y of one or more instances from their seeds' glibc rand() streams
 // (src/ising.cu:91-95, src/ising_tsp.cu:55-59), one launch.  Padded agents
-// and rows outside every instance are zero.
-int init_instances(sbx_ctx *ctx, const SolveDims &d, std::vector<RandInst> &inst, bool tsp)
+// and rows outside every instance are zero.  slot: null, or the state row of
+// each instance row (a batch class's renumbering).
+int init_instances(sbx_ctx *ctx, const SolveDims &d, std::vector<RandInst> &inst, bool tsp,
+                   const int32_t *slot = nullptr)
 {
     Work &w = ctx->w;
     cudaStream_t s = ctx->stream;
@@ -448,7 +454,7 @@ int init_instances(sbx_ctx *ctx, const SolveDims &d, std::vector<RandInst> &inst
     CK(grow(w.rinst, w.cap_rinst, inst.size()));
     CK(cudaMemcpyAsync(w.rinst, inst.data(), sizeof(RandInst) * inst.size(), cudaMemcpyHostToDevice, s));
     CK(launch_rand_init(d.prec, w.x, w.y, d.Ap, tsp, kRandChunk, w.rjump, w.rinst, (int)inst.size(),
-                        threads, s));
+                        threads, slot, s));
     // the instance table must outlive the async copy
     CK(cudaStreamSynchronize(s));
     return SBX_OK;
@@ -1046,21 +1052,39 @@ int build_class(sbx_ctx *ctx, BatchClass &c)
     std::vector<int32_t> rp((size_t)n + 1), col((size_t)nnz), rinst((size_t)n);
     std::vector<double> val((size_t)nnz);
     c.xi0.assign(ni, 0.0);
+    c.slot.assign((size_t)n, 0);
     // instances on host threads: each one's xi0 (its sums in the reference's
-    // order) and its block of the block-diagonal matrix
+    // order) and its block of the block-diagonal matrix, rows renumbered by
+    // decreasing degree (ties in row order) so that the rows a warp takes
+    // together have about the same number of neighbours; each row keeps its
+    // entries in their order, columns renamed.  Cuts, windows and integer
+    // neighbour sums do not depend on the numbering; the init and the state
+    // readback go through slot.
     const int T = nnz > (1 << 20) ? host_threads() : 1;
     parallel(T, [&](int t, int TT) {
+        std::vector<int32_t> ord, inv;
         for (size_t i = (size_t)t; i < ni; i += (size_t)TT) {
             const DevCsr &J = c.probs[i]->J;
             c.xi0[i] = xi0_of(J);
-            const int64_t r0 = c.row_off[i], e = e_off[i];
-            for (int64_t r = 0; r < J.n; r++) {
-                rp[r0 + r] = (int32_t)(e + J.hrowptr[r]);
-                rinst[r0 + r] = (int32_t)i;
-            }
-            for (int64_t k = 0; k < J.nnz; k++) {
-                col[e + k] = (int32_t)(J.hcol[k] + r0);
-                val[e + k] = J.hval[k];
+            const int64_t r0 = c.row_off[i];
+            const std::vector<int32_t> &hr = J.hrowptr;
+            ord.resize((size_t)J.n);
+            inv.resize((size_t)J.n);
+            std::iota(ord.begin(), ord.end(), 0);
+            std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) {
+                return hr[(size_t)a + 1] - hr[(size_t)a] > hr[(size_t)b + 1] - hr[(size_t)b];
+            });
+            for (int64_t k = 0; k < J.n; k++) inv[(size_t)ord[(size_t)k]] = (int32_t)k;
+            int64_t e = e_off[i];
+            for (int64_t k = 0; k < J.n; k++) {
+                const int32_t o = ord[(size_t)k];
+                rp[r0 + k] = (int32_t)e;
+                rinst[r0 + k] = (int32_t)i;
+                c.slot[(size_t)(r0 + o)] = (int32_t)(r0 + k);
+                for (int32_t j = hr[(size_t)o]; j < hr[(size_t)o + 1]; j++, e++) {
+                    col[e] = inv[(size_t)J.hcol[(size_t)j]] + (int32_t)r0;
+                    val[e] = J.hval[(size_t)j];
+                }
             }
         }
     });
@@ -1075,6 +1099,8 @@ int build_class(sbx_ctx *ctx, BatchClass &c)
     CK(cudaMalloc(&c.J.c0r32, sizeof(float) * n));
     CK(cudaMalloc(&c.J.c0r64, sizeof(double) * n));
     CK(cudaMemcpy(c.J.rinst, rinst.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&c.dslot, sizeof(int32_t) * n));
+    CK(cudaMemcpy(c.dslot, c.slot.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
     c.J.ninst = (int32_t)c.probs.size();
     CK(cudaMalloc(&c.J.iagents, sizeof(int32_t) * c.J.ninst));
     CK(cudaMalloc(&c.J.iwsum, sizeof(double) * c.J.ninst));
@@ -1379,6 +1405,7 @@ void free_batch(sbx_ctx *ctx)
         free_rb(c.rb);
         free_bsm(c.bsm);
         cudaFree(c.daoff);
+        cudaFree(c.dslot);
     }
     ctx->batch.clear();
     ctx->batch_key.clear();
@@ -1476,7 +1503,7 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
             inst[i].A = c.agents[i];
             rand_seed_window(pr->seed + (uint32_t)c.idx[i], inst[i].V0);
         }
-        if ((rc = init_instances(ctx, d, inst, false))) return rc;
+        if ((rc = init_instances(ctx, d, inst, false, c.dslot))) return rc;
         // the resident batch kernel when every instance fits a bin on chip
         int64_t maxn = 0;
         for (const sbx_problem *q : c.probs) maxn = std::max<int64_t>(maxn, q->J.n);
@@ -1521,7 +1548,7 @@ int solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems, const
         } else if (nchunks) {
             bool timed = false;
             if ((rc = pick_tile(ctx, d, c.J, pr, &timed))) return rc;
-            if (timed && (rc = init_instances(ctx, d, inst, false))) return rc;
+            if (timed && (rc = init_instances(ctx, d, inst, false, c.dslot))) return rc;
         }
         int launches = 0;
         double kms = 0;
@@ -1620,8 +1647,11 @@ float f16_to_f(uint16_t h);
 // x, y (storage values as double) and window spins of rows [row0, row0 + rows)
 // and agents [0, A) of the state in the work buffers, laid out as dims d.
 int read_state(sbx_ctx *ctx, const SolveDims &d, int64_t row0, int64_t rows, int32_t A, double *x,
-               double *y, int32_t *spins)
+               double *y, int32_t *spins, const int32_t *slot = nullptr)
 {
+    // row r of the output is state row row0 + slot[r] - row0 (slot: the
+    // global state row of each row, or null for the identity)
+    auto src_row = [&](int64_t r) { return slot ? (int64_t)slot[r] - row0 : r; };
     const size_t es = prec_bytes(d.prec), nst = (size_t)rows * d.Ap;
     std::vector<unsigned char> buf(nst * es);
     for (int which = 0; which < 2; which++) {
@@ -1631,7 +1661,7 @@ int read_state(sbx_ctx *ctx, const SolveDims &d, int64_t row0, int64_t rows, int
         CK(cudaMemcpy(buf.data(), src, nst * es, cudaMemcpyDeviceToHost));
         for (int64_t r = 0; r < rows; r++)
             for (int a = 0; a < A; a++) {
-                const size_t i = (size_t)r * d.Ap + a;
+                const size_t i = (size_t)src_row(r) * d.Ap + a;
                 double v;
                 if (d.prec == P_F64) memcpy(&v, &buf[i * 8], 8);
                 else if (d.prec == P_F32) {
@@ -1651,7 +1681,7 @@ int read_state(sbx_ctx *ctx, const SolveDims &d, int64_t row0, int64_t rows, int
         CK(cudaMemcpy(pl.data(), ctx->w.Wp + (size_t)row0 * d.W, pl.size() * 4, cudaMemcpyDeviceToHost));
         for (int64_t r = 0; r < rows; r++)
             for (int a = 0; a < A; a++)
-                spins[(size_t)r * A + a] = ((pl[(size_t)r * d.W + a / 32] >> (a % 32)) & 1u) ? -1 : 1;
+                spins[(size_t)r * A + a] = ((pl[(size_t)src_row(r) * d.W + a / 32] >> (a % 32)) & 1u) ? -1 : 1;
     }
     return SBX_OK;
 }
@@ -2063,7 +2093,8 @@ int sbx_get_batch_state(sbx_ctx *ctx, int32_t index, double *x, double *y, int32
     for (size_t i = 0; i < c.idx.size(); i++)
         if (c.idx[i] == index) {
             CK(cudaSetDevice(ctx->device));
-            return read_state(ctx, ctx->d, c.row_off[i], c.probs[i]->J.n, c.agents[i], x, y, spins);
+            return read_state(ctx, ctx->d, c.row_off[i], c.probs[i]->J.n, c.agents[i], x, y, spins,
+                              c.slot.data() + c.row_off[i]);
         }
     return fail(ctx, SBX_ERR_STATE, "instance not in the last agent class solved (its state was overwritten)");
 }

@@ -195,9 +195,10 @@ void rand_seed_window(uint32_t seed, uint32_t *V0);
 // out[b] = M^(L * 2^b), b < nbits (31x31 each): independent of the seed.
 void rand_jump_matrices(int64_t L, int nbits, std::vector<uint32_t> &out);
 int rand_threads_bits(int64_t outputs, int64_t L);
+// slot: null, or (batched MaxCut) the state row of each instance row.
 cudaError_t launch_rand_init(int prec, void *x, void *y, int32_t Ap, bool tsp, int64_t L,
                              const uint32_t *mats, const RandInst *inst, int count,
-                             int64_t total_threads, cudaStream_t s);
+                             int64_t total_threads, const int32_t *slot, cudaStream_t s);
 
 // Streaming MaxCut kernels (k_stream.cu).
 cudaError_t launch_prestep(const SolveDims &d, const DevCsr &J, Work &w, cudaStream_t s,

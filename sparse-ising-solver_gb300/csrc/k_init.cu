@@ -88,11 +88,14 @@ template <class T>
 __device__ __forceinline__ void put(T *p, int64_t i, double v) { p[i] = St<T>::st((typename St<T>::A)v); }
 
 // One thread: find its instance, jump to its chunk start, emit L outputs.
+// slot (MaxCut only, may be null): the row of the state that takes the
+// instance's row r, as a global row (row_off + r -> slot[row_off + r]).
 template <class T>
 __global__ void __launch_bounds__(128) k_rand_init(T *x, T *y, int32_t Ap, int tsp, int64_t L,
                                                    const uint32_t *__restrict__ mats,
                                                    const RandInst *__restrict__ inst, int count,
-                                                   int64_t total_threads)
+                                                   int64_t total_threads,
+                                                   const int32_t *__restrict__ slot)
 {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= total_threads) return;
@@ -144,7 +147,9 @@ __global__ void __launch_bounds__(128) k_rand_init(T *x, T *y, int32_t Ap, int t
                     put(xi, idx, 0.0);
                     put(yi, idx, val);
                 } else {
-                    const int64_t e = o >> 1, row = e / A, a = e - row * A, idx = row * Ap + a;
+                    const int64_t e = o >> 1, row = e / A, a = e - row * A;
+                    const int64_t srow = slot ? (int64_t)__ldg(&slot[I.row_off + row]) - I.row_off : row;
+                    const int64_t idx = srow * Ap + a;
                     if (o & 1) put(yi, idx, val);
                     else put(xi, idx, val);
                 }
@@ -156,13 +161,14 @@ __global__ void __launch_bounds__(128) k_rand_init(T *x, T *y, int32_t Ap, int t
 
 template <class T>
 cudaError_t launch_t(void *x, void *y, int32_t Ap, int tsp, int64_t L, const uint32_t *mats,
-                     const RandInst *inst, int count, int64_t total_threads, cudaStream_t s)
+                     const RandInst *inst, int count, int64_t total_threads, const int32_t *slot,
+                     cudaStream_t s)
 {
     const int blk = 128;
     const int64_t grid = (total_threads + blk - 1) / blk;
     if (grid == 0) return cudaSuccess;
     k_rand_init<T><<<(unsigned)grid, blk, 0, s>>>((T *)x, (T *)y, Ap, tsp, L, mats, inst, count,
-                                                 total_threads);
+                                                 total_threads, slot);
     return cudaGetLastError();
 }
 
@@ -170,13 +176,15 @@ cudaError_t launch_t(void *x, void *y, int32_t Ap, int tsp, int64_t L, const uin
 
 cudaError_t launch_rand_init(int prec, void *x, void *y, int32_t Ap, bool tsp, int64_t L,
                              const uint32_t *mats, const RandInst *inst, int count,
-                             int64_t total_threads, cudaStream_t s)
+                             int64_t total_threads, const int32_t *slot, cudaStream_t s)
 {
+    if (tsp) slot = nullptr;
     switch (prec) {
-    case P_F32: return launch_t<float>(x, y, Ap, tsp, L, mats, inst, count, total_threads, s);
-    case P_BF16: return launch_t<__nv_bfloat16>(x, y, Ap, tsp, L, mats, inst, count, total_threads, s);
-    case P_F16: return launch_t<__half>(x, y, Ap, tsp, L, mats, inst, count, total_threads, s);
-    default: return launch_t<double>(x, y, Ap, tsp, L, mats, inst, count, total_threads, s);
+    case P_F32: return launch_t<float>(x, y, Ap, tsp, L, mats, inst, count, total_threads, slot, s);
+    case P_BF16:
+        return launch_t<__nv_bfloat16>(x, y, Ap, tsp, L, mats, inst, count, total_threads, slot, s);
+    case P_F16: return launch_t<__half>(x, y, Ap, tsp, L, mats, inst, count, total_threads, slot, s);
+    default: return launch_t<double>(x, y, Ap, tsp, L, mats, inst, count, total_threads, slot, s);
     }
 }
 
