@@ -78,7 +78,7 @@ TRAFFIC = {
     # per SB step: the k_row launch plus 1/100 of the isolated rows' k_iso
     "rmat20": (9.814e8, "ncu --set full -k regex:k_row|k_iso: bench.py --workload rmat20 "
                         "--profile 100 (k_row launch + k_iso / 100)"),
-    "batch512": (1.0659e9, "ncu --set full -k regex:k_bsm -s 4 -c 1: bench.py --workload batch512 "
+    "batch512": (1.0662e9, "ncu --set full -k regex:k_bsm -s 4 -c 1: bench.py --workload batch512 "
                            "--profile 100 (one k_bsm launch)"),
     # the whole 2,000-step solve is one launch; per launch of the bench's
     # 20,000-step solve the state read once is the same

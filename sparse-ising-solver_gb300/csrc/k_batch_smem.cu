@@ -88,8 +88,14 @@ __global__ void __launch_bounds__(NT, 1) k_bsm(const StepP P, const BsmP B, cons
             // the instance's plane (written by the previous step) and the
             // all-zero row that padded neighbours read
             __syncthreads();
+            // (cp.async: a thread issues all its word copies back to back and
+            // waits once, instead of a load-to-store round trip per word)
             const uint32_t *src = Scur + (int64_t)__ldg(&B.ioff[inst]) * W;
-            for (int i = tid; i < ni * W; i += NT) s_plane[i] = __ldcg(src + i);
+            const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(s_plane);
+            for (int i = tid; i < ni * W; i += NT)
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 4;"
+                             :: "r"(sbase + 4u * (uint32_t)i), "l"(src + i) : "memory");
+            asm volatile("cp.async.wait_all;" ::: "memory");
             if (tid < W) s_plane[ni * W + tid] = 0u;
             __syncthreads();
             loaded = inst;
