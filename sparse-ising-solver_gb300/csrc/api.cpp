@@ -1204,8 +1204,9 @@ bool bsm_ok(const BatchClass &c, const SolveDims &d)
 // The plan: columns as byte offsets into the instance's plane, and the rows
 // (in instance order) cut into one contiguous run per CTA of about equal
 // cost, each run split at instance boundaries.  A row costs its neighbours
-// plus the update of its agents (about 48 neighbour loads' worth at 64
-// agents, measured by instruction counts of the kernel's loops).
+// plus the update of its agents, 20 (W + 1) neighbours' worth (timed on
+// GB300 for batch512 at 64 agents: 240.7 us a step, against 243.0 with
+// 16 (W + 1), 242.4 with 24 (W + 1) and 263.1 with 8 (W + 1)).
 int build_bsm(sbx_ctx *ctx, BatchClass &c, int W)
 {
     DevBsm &M = c.bsm;
@@ -1258,7 +1259,7 @@ int build_bsm(sbx_ctx *ctx, BatchClass &c, int W)
     });
     if (outside) return fail(ctx, SBX_ERR_ARG, "batch: a column outside its instance");
     const int grid = std::max(1, dev_attr(cudaDevAttrMultiProcessorCount));
-    const double row_cost = 16.0 * W + 16.0;
+    const double row_cost = 20.0 * W + 20.0;
     double total = 0;
     for (int64_t r = 0; r < n; r++) total += row_cost + (c.J.hrowptr[(size_t)r + 1] - c.J.hrowptr[(size_t)r]);
     std::vector<int32_t> seg, cta((size_t)grid + 1, 0);
