@@ -202,7 +202,8 @@ int sbx_solve_batch(sbx_ctx *ctx, int32_t count, sbx_problem *const *problems,
                     double *batch_time_us);
 
 /* State of instance `index` (its position in the last sbx_solve_batch
- * call), as sbx_get_state: x, y, spins [n_i * agents_i] each, row-major.
+ * call), as sbx_get_state: x, y, spins [n_i * agents_i] each, row-major in
+ * the instance's own row order (the batch renumbers rows internally).
  * No counterpart in the reference (it has no batched solve).  Instances are
  * solved one agent class (padded agent count) after another in the same
  * buffers, so only the last class's instances are available; others give
