@@ -68,6 +68,13 @@ RESTART_ROWS = 0.1
 RESTART_MAX_COPIES = 32
 
 
+def restart_copies(rows_missed, rows_total):
+    """Copies of each missed instance in a restart round: as many as keep the
+    round's batch near RESTART_ROWS of the full batch's rows, at least one
+    and at most RESTART_MAX_COPIES."""
+    return int(min(RESTART_MAX_COPIES, max(1, RESTART_ROWS * rows_total // max(1, rows_missed))))
+
+
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of
 # each workload's dominant kernel, from one ncu capture of the same kernel
 # and tile (the command is in the source string); the resident kernels'
@@ -914,8 +921,7 @@ def run_batch(args, wl, rank, world, local):
         t_restart = float(rt[0]["time_us"]) if rt[0]["time_us"] > 0 else None
         while len(missed) and rounds < 8 and t_restart is not None:
             rounds += 1
-            rows_missed = sum(graphs[i].n for i in missed)
-            copies = int(min(RESTART_MAX_COPIES, max(1, RESTART_ROWS * n_tot // rows_missed)))
+            copies = restart_copies(sum(graphs[i].n for i in missed), n_tot)
             copies_used.append(copies)
             rep = np.repeat(missed, copies)
             rr, _, t_sub = ctx.solve_batch([probs[i] for i in rep], [A] * len(rep), sbx.params(

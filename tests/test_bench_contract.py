@@ -57,3 +57,20 @@ def test_reference_arm_batch_loads_no_engine_code():
     assert d["config"]["workload"].startswith("batch-512")
     assert "12 instances" in d["cpu_baseline"]["sample"]
     assert "MAPS 0" in p.stdout
+
+
+def test_restart_copies_keep_a_round_near_a_tenth_of_the_batch():
+    # the batch time-to-target's restart rounds: copies of each missed
+    # instance sized to the round's rows, clamped to [1, 32]
+    sys.path.insert(0, ROOT)
+    import bench
+    n = 1_908_368
+    assert bench.restart_copies(139_000, n) == 1      # many misses: one copy each
+    assert bench.restart_copies(50_000, n) == 3
+    assert bench.restart_copies(5_000, n) == 32       # a few small ones: the cap
+    assert bench.restart_copies(n, n) == 1
+    assert bench.restart_copies(0, n) == 32           # nothing missed: never divides by zero
+    for rows in (100, 1_000, 10_000, 100_000, 1_000_000):
+        c = bench.restart_copies(rows, n)
+        assert 1 <= c <= bench.RESTART_MAX_COPIES
+        assert c == 1 or c * rows <= bench.RESTART_ROWS * n
